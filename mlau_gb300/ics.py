@@ -1,0 +1,240 @@
+"""Seeded synthetic initial conditions for the solver's benchmark workloads.
+
+The reference ships no datasets; its problems are analytic.  These generators
+produce host arrays in the reference layout (one float64 array per variable,
+x fastest, ``off`` ghost cells per side, ghosts filled periodically) for:
+
+* ``riemann_1d``  - a seeded 1D Riemann problem (2048 cells, discontinuity at
+  x=0.5; left/right rho,p ~ U[0.1,1], v ~ U[-1,1]^3, By,Bz ~ U[-1,1], shared
+  Bx ~ U[0.5,1], gamma=2).
+* ``turbulence_2d`` - a periodic [0,1]^2 box: rho=1, p=1/gamma, velocity and
+  Az each a sum of 16 random-phase Fourier modes with 0<|k|<=8 and amplitude
+  ~|k|^-2; v_rms set, B_rms from plasma beta.
+* ``turbulence_3d`` - a periodic [0,1]^3 box: rho=1 with a 1% random-phase
+  perturbation (|k|<=6), solenoidal random-phase velocity at a given rms sonic
+  Mach, B = B0 + curl A with A at 10% of |B0|, beta=1 w.r.t. |B0|^2.
+
+Face-centred B is built as the discrete curl of an edge-centred vector
+potential with the scheme's own face-to-centre difference (2-point for
+order<=2, the (27,-1)/24 stencil for order>=3, reference mhd_fd_ct_3d.c:80-88),
+so the scheme's discrete div B vanishes to round-off from the first step.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+VARS3 = ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")
+VARS1 = ("ro", "mx", "my", "mz", "en", "by", "bz")
+
+
+def _modes(rng, ndim, nmodes, kmax):
+    """Random integer wave vectors with 0 < |k| <= kmax."""
+    out = []
+    while len(out) < nmodes:
+        k = rng.integers(-kmax, kmax + 1, size=ndim)
+        kk = float(np.sqrt((k * k).sum()))
+        if 0 < kk <= kmax:
+            out.append(k)
+    return np.array(out, dtype=np.int64)
+
+
+def _field(rng, coords, nmodes, kmax, slope=-2.0):
+    """Sum of random-phase cosine modes, amplitude ~ |k|^slope, on `coords`
+    (tuple of broadcastable coordinate arrays in [0,1))."""
+    ks = _modes(rng, len(coords), nmodes, kmax)
+    phases = rng.uniform(0.0, 2.0 * np.pi, size=nmodes)
+    f = 0.0
+    for k, ph in zip(ks, phases):
+        arg = sum(2.0 * np.pi * float(kc) * c for kc, c in zip(k, coords)) + ph
+        f = f + (float(np.sqrt((k * k).sum())) ** slope) * np.cos(arg)
+    return f
+
+
+def _ddx(f, axis, n, odr):
+    """Scheme difference of a periodic staggered field along `axis`: value at
+    index i uses f[i-1..i+2] (face-to-centre or edge-to-face), divided by 1/n."""
+    f1 = f
+    f2 = np.roll(f, -1, axis=axis)
+    if odr <= 2:
+        d = f2 - f1
+    else:
+        f0 = np.roll(f, 1, axis=axis)
+        f3 = np.roll(f, -2, axis=axis)
+        d = (27.0 * (f2 - f1) - (f3 - f0)) / 24.0
+    return d * n
+
+
+def _center(f, axis, odr):
+    """Scheme face-to-centre average (calc_bc) of a periodic face field."""
+    f1 = f
+    f2 = np.roll(f, -1, axis=axis)
+    if odr <= 2:
+        return 0.5 * (f1 + f2)
+    f0 = np.roll(f, 1, axis=axis)
+    f3 = np.roll(f, -2, axis=axis)
+    return 0.0625 * (9.0 * (f1 + f2) - (f0 + f3))
+
+
+def pad_periodic(f, off):
+    return np.ascontiguousarray(np.pad(f, off, mode="wrap"))
+
+
+def turbulence_3d(n=64, mach=1e-2, seed=0, off=4, gamma=5.0 / 3.0, odr=4, ny=None, nz=None,
+                  b0=(1.0, 0.5, 0.0), a_frac=0.1, beta=1.0, rho_pert=0.01, nmodes=16):
+    """Config-3 workload.  Returns (state dict of padded arrays, meta dict)."""
+    nx = n
+    ny = ny or n
+    nz = nz or n
+    rng = np.random.default_rng(seed)
+    ic = (np.arange(nx) + 0.5) / nx
+    jc = (np.arange(ny) + 0.5) / ny
+    kc = (np.arange(nz) + 0.5) / nz
+    ifc, jfc, kfc = np.arange(nx) / nx, np.arange(ny) / ny, np.arange(nz) / nz
+    Z, Y, X = np.meshgrid(kc, jc, ic, indexing="ij")
+    B0 = np.array(b0, dtype=np.float64)
+    b0abs = float(np.sqrt((B0 * B0).sum()))
+    p0 = beta * 0.5 * b0abs ** 2
+
+    # density: 1 + 1% random-phase perturbation with |k|<=6
+    dr = _field(rng, (X, Y, Z), nmodes, 6)
+    ro = 1.0 + rho_pert * dr / np.sqrt(np.mean(dr * dr))
+
+    # solenoidal velocity: v = curl(psi), analytic per mode
+    cs = np.sqrt(gamma * p0 / 1.0)
+    v = [np.zeros_like(X) for _ in range(3)]
+    ks = _modes(rng, 3, nmodes, 8)
+    for k in ks:
+        amp = rng.normal(size=3) * float(np.sqrt((k * k).sum())) ** -2.0
+        ph = rng.uniform(0, 2 * np.pi)
+        arg = 2 * np.pi * (k[0] * X + k[1] * Y + k[2] * Z) + ph
+        s = -2 * np.pi * np.sin(arg)
+        kxp = np.cross(k.astype(np.float64), amp)  # k x psi_k
+        for c in range(3):
+            v[c] = v[c] + kxp[c] * s
+    vr = np.sqrt(np.mean(v[0] ** 2 + v[1] ** 2 + v[2] ** 2))
+    v = [c * (mach * cs / vr) for c in v]
+
+    # vector potential on edges: Ax at (i, j-1/2, k-1/2), Ay at (i-1/2, j, k-1/2),
+    # Az at (i-1/2, j-1/2, k); B = B0 + curl A on faces with the scheme difference
+    Zax, Yax, Xax = np.meshgrid(kfc, jfc, ic, indexing="ij")
+    Zay, Yay, Xay = np.meshgrid(kfc, jc, ifc, indexing="ij")
+    Zaz, Yaz, Xaz = np.meshgrid(kc, jfc, ifc, indexing="ij")
+    fa = [_field(rng, (Xax, Yax, Zax), nmodes, 6),
+          _field(rng, (Xay, Yay, Zay), nmodes, 6),
+          _field(rng, (Xaz, Yaz, Zaz), nmodes, 6)]
+    # arrays are (z, y, x): axis 2 = x, 1 = y, 0 = z.  Differences land one
+    # half-cell over, matching the face the component lives on.
+    bx = _ddx(fa[2], 1, ny, odr) - _ddx(fa[1], 0, nz, odr)
+    by = _ddx(fa[0], 0, nz, odr) - _ddx(fa[2], 2, nx, odr)
+    bz = _ddx(fa[1], 2, nx, odr) - _ddx(fa[0], 1, ny, odr)
+    brms = np.sqrt(np.mean(bx ** 2 + by ** 2 + bz ** 2))
+    scale = a_frac * b0abs / brms
+    bx = B0[0] + bx * scale
+    by = B0[1] + by * scale
+    bz = B0[2] + bz * scale
+    cxc = _center(bx, 2, odr)
+    cyc = _center(by, 1, odr)
+    czc = _center(bz, 0, odr)
+    en = p0 / (gamma - 1.0) + 0.5 * (ro * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2)
+                                     + (cxc ** 2 + cyc ** 2 + czc ** 2))
+    st = {"ro": ro, "mx": ro * v[0], "my": ro * v[1], "mz": ro * v[2], "en": en,
+          "bx": bx, "by": by, "bz": bz}
+    st = {k: pad_periodic(a, off) for k, a in st.items()}
+    meta = dict(dx=1.0 / nx, dy=1.0 / ny, dz=1.0 / nz, gamma=gamma, off=off, p0=p0, mach=mach,
+                cs=cs, vfast=float(np.sqrt(gamma * p0 + b0abs ** 2)) + mach * cs)
+    return st, meta
+
+
+def turbulence_2d(n=512, seed=0, off=4, gamma=5.0 / 3.0, odr=4, ny=None, vrms=0.5, beta=1.0,
+                  nmodes=16, kmax=8):
+    """Config-2 workload: 2D periodic box; returns (state, meta)."""
+    nx = n
+    ny = ny or n
+    rng = np.random.default_rng(seed)
+    ic = (np.arange(nx) + 0.5) / nx
+    jc = (np.arange(ny) + 0.5) / ny
+    ifc, jfc = np.arange(nx) / nx, np.arange(ny) / ny
+    Y, X = np.meshgrid(jc, ic, indexing="ij")
+    p0 = 1.0 / gamma
+    vx = _field(rng, (X, Y), nmodes, kmax)
+    vy = _field(rng, (X, Y), nmodes, kmax)
+    r = np.sqrt(np.mean(vx ** 2 + vy ** 2))
+    vx, vy = vx * (vrms / r), vy * (vrms / r)
+    # Az at cell corners (i-1/2, j-1/2)
+    Yc, Xc = np.meshgrid(jfc, ifc, indexing="ij")
+    az = _field(rng, (Xc, Yc), nmodes, kmax)
+    bx = _ddx(az, 0, ny, odr)
+    by = -_ddx(az, 1, nx, odr)
+    b2 = np.mean(_center(bx, 1, odr) ** 2 + _center(by, 0, odr) ** 2)
+    scale = np.sqrt(2.0 * p0 / beta / b2)
+    bx, by = bx * scale, by * scale
+    bz = np.zeros_like(bx)
+    ro = np.ones_like(vx)
+    cxc, cyc = _center(bx, 1, odr), _center(by, 0, odr)
+    en = p0 / (gamma - 1.0) + 0.5 * (ro * (vx ** 2 + vy ** 2) + (cxc ** 2 + cyc ** 2))
+    st = {"ro": ro, "mx": ro * vx, "my": ro * vy, "mz": np.zeros_like(vx), "en": en,
+          "bx": bx, "by": by, "bz": bz}
+    st = {k: pad_periodic(a, off) for k, a in st.items()}
+    meta = dict(dx=1.0 / nx, dy=1.0 / ny, gamma=gamma, off=off, p0=p0,
+                vfast=float(np.sqrt(gamma * p0 + 2.0 * p0 / beta)) + vrms)
+    return st, meta
+
+
+def riemann_1d(n=2048, seed=0, off=4, gamma=2.0):
+    """Config-1 workload: seeded 1D Riemann problem on [0,1]; returns (state, meta)."""
+    rng = np.random.default_rng(seed)
+    nx = n + 2 * off
+    dx = 1.0 / n
+    x = (np.arange(nx) - off + 0.5) * dx
+    left = x <= 0.5
+    rl, rr = rng.uniform(0.1, 1.0, 2)
+    pl, pr = rng.uniform(0.1, 1.0, 2)
+    vl = rng.uniform(-1, 1, 3)
+    vrr = rng.uniform(-1, 1, 3)
+    bl = rng.uniform(-1, 1, 2)
+    br = rng.uniform(-1, 1, 2)
+    bx = float(rng.uniform(0.5, 1.0))
+    ro = np.where(left, rl, rr)
+    p = np.where(left, pl, pr)
+    v = [np.where(left, vl[c], vrr[c]) for c in range(3)]
+    by = np.where(left, bl[0], br[0])
+    bz = np.where(left, bl[1], br[1])
+    en = p / (gamma - 1) + 0.5 * (ro * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2)
+                                  + (bx * bx + by * by + bz * bz))
+    st = {"ro": ro, "mx": ro * v[0], "my": ro * v[1], "mz": ro * v[2], "en": en, "by": by,
+          "bz": bz}
+    st = {k: np.ascontiguousarray(a, dtype=np.float64) for k, a in st.items()}
+    return st, dict(bx=bx, dx=dx, gamma=gamma, off=off)
+
+
+def copy_state(s):
+    return {k: v.copy() for k, v in s.items()}
+
+
+def div_b_3d(st, dx, dy, dz, off=4, odr=4):
+    """max |div B| * dx / max|B| over interior cells with the scheme difference."""
+    def d(f, ax, h):
+        f1 = f
+        f2 = np.roll(f, -1, axis=ax)
+        if odr <= 2:
+            return (f2 - f1) / h
+        f0, f3 = np.roll(f, 1, axis=ax), np.roll(f, -2, axis=ax)
+        return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0 / h
+    div = d(st["bx"], 2, dx) + d(st["by"], 1, dy) + d(st["bz"], 0, dz)
+    sl = (slice(off, -off),) * 3
+    bmax = max(np.abs(st[k][sl]).max() for k in ("bx", "by", "bz"))
+    return float(np.abs(div[sl]).max() * min(dx, dy, dz) / bmax)
+
+
+def div_b_2d(st, dx, dy, off=4, odr=4):
+    def d(f, ax, h):
+        f1 = f
+        f2 = np.roll(f, -1, axis=ax)
+        if odr <= 2:
+            return (f2 - f1) / h
+        f0, f3 = np.roll(f, 1, axis=ax), np.roll(f, -2, axis=ax)
+        return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0 / h
+    div = d(st["bx"], 1, dx) + d(st["by"], 0, dy)
+    sl = (slice(off, -off),) * 2
+    bmax = max(np.abs(st[k][sl]).max() for k in ("bx", "by"))
+    return float(np.abs(div[sl]).max() * min(dx, dy) / bmax)

@@ -1,0 +1,152 @@
+"""CPU oracles for the MLAU hot path.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
+import this package, and only as the checker.  Two oracles:
+
+* ``Port`` - the C restatement in this directory (mlau_oracle.c), built on
+  any host by ``build.build_port()``.
+* ``Ref`` - the reference's own drivers compiled from its sources by
+  ``build.build_ref_variant()``; available only where the reference tree is.
+
+Both take numpy float64 arrays (one per variable, x fastest) and update them
+in place, exactly like the reference drivers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import numpy as np
+
+from . import build
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_cdp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+FLUX = {"mlau": 0, "lhlld": 1, "hlld": 2, "roe": 3}
+
+
+def _flux_id(f):
+    return FLUX[f] if isinstance(f, str) else int(f)
+
+
+class Port:
+    """ctypes binding of oracle/_build/liboracle.so."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            lib = C.CDLL(build.build_port())
+            d, i = C.c_double, C.c_int
+            lib.oracle_fd_ct_3d.argtypes = [_dp] * 8 + [d, d, d, d] + [i] * 6 + [d, i, i, i]
+            lib.oracle_fd_ct_3d.restype = None
+            lib.oracle_fd_ct_2d.argtypes = [_dp] * 8 + [d, d, d] + [i] * 4 + [d, i, i, i]
+            lib.oracle_fd_ct_2d.restype = None
+            lib.oracle_fd4c_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d, i, i, i, i]
+            lib.oracle_fd4c_1d.restype = None
+            lib.oracle_cfl_3d.argtypes = [_cdp] * 8 + [i] * 6 + [d, d, d, d, d, C.POINTER(d)]
+            lib.oracle_cfl_3d.restype = d
+            lib.oracle_cfl_2d.argtypes = [_cdp] * 8 + [i] * 4 + [d, d, d, d, d, C.POINTER(d)]
+            lib.oracle_cfl_2d.restype = d
+            lib.oracle_dt_1d.argtypes = [_cdp] * 7 + [d, i, d, d, d, d]
+            lib.oracle_dt_1d.restype = d
+            lib.oracle_rec_lr.argtypes = [i, _cdp, C.POINTER(d), C.POINTER(d)]
+            lib.oracle_flux.argtypes = [i, _cdp, _cdp, _dp]
+            lib.oracle_reconst.argtypes = [i, i, _cdp, d, d, _dp, _dp]
+            cls._lib = lib
+        return cls._lib
+
+    @classmethod
+    def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3):
+        nz, ny, nx = s["ro"].shape
+        cls.lib().oracle_fd_ct_3d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                  dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma, odr,
+                                  _flux_id(flux), nrk)
+
+    @classmethod
+    def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3):
+        ny, nx = s["ro"].shape
+        cls.lib().oracle_fd_ct_2d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                  dt, dx, dy, nx, ny, off, off, gamma, odr, _flux_id(flux), nrk)
+
+    @classmethod
+    def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open"):
+        nx = s["ro"].shape[0]
+        cls.lib().oracle_fd4c_1d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")],
+                                 bx, dt, dx, nx, off, gamma, odr, _flux_id(flux), nrk,
+                                 0 if bc == "open" else 1)
+
+    @classmethod
+    def cfl3d(cls, s, cfl, dr, vfast, dt_old, off=4, gamma=5 / 3):
+        nz, ny, nx = s["ro"].shape
+        vm = C.c_double()
+        dt = cls.lib().oracle_cfl_3d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                     nx, ny, nz, off, off, off, gamma, cfl, dr, vfast, dt_old,
+                                     C.byref(vm))
+        return dt, vm.value
+
+    @classmethod
+    def cfl2d(cls, s, cfl, dr, vfast, dt_old, off=4, gamma=5 / 3):
+        ny, nx = s["ro"].shape
+        vm = C.c_double()
+        dt = cls.lib().oracle_cfl_2d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                     nx, ny, off, off, gamma, cfl, dr, vfast, dt_old, C.byref(vm))
+        return dt, vm.value
+
+    @classmethod
+    def dt1d(cls, s, bx, gamma, cfl, dx, vfloor=1.0):
+        nx = s["ro"].shape[0]
+        return cls.lib().oracle_dt_1d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")],
+                                      bx, nx, gamma, cfl, dx, vfloor)
+
+    @classmethod
+    def flux(cls, which, left7, right7, bn, gamma, dv=(0.0, 0.0)):
+        inp = np.ascontiguousarray(np.r_[left7, right7, bn, gamma], dtype=np.float64)
+        out = np.zeros(7)
+        cls.lib().oracle_flux(_flux_id(which), inp, np.ascontiguousarray(dv, dtype=np.float64), out)
+        return out
+
+
+class Ref:
+    """ctypes binding of a reference-driver variant built into oracle/_ref."""
+
+    _libs: dict = {}
+
+    @staticmethod
+    def available() -> bool:
+        return build.reference_available()
+
+    @classmethod
+    def _get(cls, dim, odr, flux, nrk, bc="open"):
+        key = (dim, odr, flux, nrk, bc if dim == 1 else "")
+        if key not in cls._libs:
+            lib = C.CDLL(build.build_ref_variant(dim, odr, flux, nrk, bc))
+            d, i = C.c_double, C.c_int
+            if dim == 1:
+                lib.ref_step_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d]
+                lib.ref_step_1d.restype = None
+            else:
+                lib.ref_step.argtypes = [_dp] * 8 + [d, d, d, d] + [i] * 6 + [d]
+                lib.ref_step.restype = None
+            cls._libs[key] = lib
+        return cls._libs[key]
+
+    @classmethod
+    def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3):
+        nz, ny, nx = s["ro"].shape
+        cls._get(3, odr, _flux_id(flux), nrk).ref_step(
+            *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+            dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma)
+
+    @classmethod
+    def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3):
+        ny, nx = s["ro"].shape
+        cls._get(2, odr, _flux_id(flux), nrk).ref_step(
+            *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+            dt, dx, dy, 1.0, nx, ny, 1, off, off, 0, gamma)
+
+    @classmethod
+    def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open"):
+        nx = s["ro"].shape[0]
+        cls._get(1, odr, _flux_id(flux), nrk, bc).ref_step_1d(
+            *[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")], bx, dt, dx, nx, off, gamma)

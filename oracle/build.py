@@ -1,0 +1,137 @@
+"""Build recipes for the two CPU oracles.  TEST INFRASTRUCTURE ONLY.
+
+* ``build_port()`` compiles this directory's C restatement
+  (mlau_oracle.c) into ``oracle/_build/liboracle.so``.  It needs only gcc and
+  works on any host, including the GPU machine.
+* ``build_ref_variant(...)`` compiles the reference's own driver and boundary
+  sources, read where they lie under the reference tree, into
+  ``oracle/_ref/``.  The reference selects its scheme with ``#define`` lines
+  and an uncommented ``func_flux=`` assignment inside each driver, so the
+  recipe writes sed-style patched copies of those files into
+  ``oracle/_ref/src/<variant>/`` (build intermediates, never committed) and
+  compiles them with ``-O2 -fopenmp -ffp-contract=off`` (the reference's own
+  flags, Makefile.inc:4, plus an explicit no-contraction flag) and the
+  single-rank ``ref_stub/mpi.h``.
+
+Usage: ``python oracle/build.py [--port] [--ref-all]``.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REF_ROOT = os.environ.get("MLAU_REFERENCE_ROOT", "/root/reference")
+
+FLUX_NAMES = {0: "mlau", 1: "lhlld", 2: "hlld", 3: "roe"}
+CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def port_path() -> str:
+    return os.path.join(BUILD, "liboracle.so")
+
+
+def build_port(force: bool = False) -> str:
+    """Compile the C restatement; return the shared library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = port_path()
+    srcs = [os.path.join(HERE, f) for f in ("mlau_oracle.c", "mlau_oracle.h", "oracle_point.h")]
+    if not force and os.path.exists(out):
+        if os.path.getmtime(out) >= max(os.path.getmtime(s) for s in srcs):
+            return out
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-std=gnu11", *CFLAGS, "-o", tmp, os.path.join(HERE, "mlau_oracle.c"), "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, out)
+    return out
+
+
+def reference_available() -> bool:
+    return os.path.isfile(os.path.join(REF_ROOT, "include", "mhd_flux.h"))
+
+
+def _variant_name(dim: int, odr: int, flux: int, nrk: int, bc: str) -> str:
+    return f"ref{dim}d_o{odr}_{FLUX_NAMES[flux]}_rk{nrk}" + (f"_{bc}" if dim == 1 else "")
+
+
+def _patch_driver(text: str, odr: int, flux: int, nrk: int) -> str:
+    text, n1 = re.subn(r"^#define ODR \(\d\)", f"#define ODR ({odr})", text, count=1, flags=re.M)
+    text, n2 = re.subn(r"^#define R_K \(\d\)", f"#define R_K ({nrk})", text, count=1, flags=re.M)
+    text, n3 = re.subn(r"^(\s*)func_flux=&calc_flux_lhlld;",
+                       lambda m: f"{m.group(1)}func_flux=&calc_flux_{FLUX_NAMES[flux]};",
+                       text, count=1, flags=re.M)
+    if (n1, n2, n3) != (1, 1, 1):
+        raise RuntimeError("reference driver layout not recognised; patch failed")
+    return text
+
+
+def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
+                      bc: str = "open") -> str:
+    """Compile one scheme variant of the reference driver; return the .so path.
+
+    dim 3: 3D/MPI/OTvortex/{mhd_fd_ct_3d.c,boundary.c}
+    dim 2: 2D/SERIAL/OTvortex/{mhd_fd_ct_2d.c,boundary.c}
+    dim 1: 1D/SERIAL/shock/{mhd_fd4c_1d.c,openbc1d_mhd.c} (bc="open") or
+           1D/SERIAL/wave/{mhd_fd4c_1d.c,prdc_1d.c} (bc="periodic")
+    """
+    if not reference_available():
+        raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
+    name = _variant_name(dim, odr, flux, nrk, bc)
+    out = os.path.join(REF_OUT, f"lib{name}.so")
+    if os.path.exists(out):
+        return out
+    if dim == 3:
+        d, drv, extra = "3D/MPI/OTvortex", "mhd_fd_ct_3d.c", ["boundary.c"]
+    elif dim == 2:
+        d, drv, extra = "2D/SERIAL/OTvortex", "mhd_fd_ct_2d.c", ["boundary.c"]
+    elif bc == "open":
+        d, drv, extra = "1D/SERIAL/shock", "mhd_fd4c_1d.c", ["openbc1d_mhd.c"]
+    else:
+        d, drv, extra = "1D/SERIAL/wave", "mhd_fd4c_1d.c", ["prdc_1d.c"]
+    src_dir = os.path.join(REF_OUT, "src", name)
+    os.makedirs(src_dir, exist_ok=True)
+    with open(os.path.join(REF_ROOT, d, drv)) as fh:
+        patched = _patch_driver(fh.read(), odr, flux, nrk)
+    drv_copy = os.path.join(src_dir, drv.replace(".c", ".cpp"))
+    with open(drv_copy, "w") as fh:
+        fh.write(patched)
+    srcs = [drv_copy] + [os.path.join(REF_ROOT, d, e) for e in extra]
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["g++", "-x", "c++", *CFLAGS, f"-DREF_DIM={dim}",
+           "-I" + os.path.join(REF_ROOT, "include"), "-I" + os.path.join(HERE, "ref_stub"),
+           "-o", tmp, *srcs, os.path.join(HERE, "ref_harness.cpp"), "-lm"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+    os.replace(tmp, out)
+    return out
+
+
+def all_variants():
+    for dim in (3, 2):
+        for odr in (1, 2, 3, 4):
+            for flux in (0, 1, 2, 3):
+                yield dict(dim=dim, odr=odr, flux=flux, nrk=3)
+        for nrk in (1, 2):
+            yield dict(dim=dim, odr=4, flux=0, nrk=nrk)
+    for bc in ("open", "periodic"):
+        for odr in (1, 2, 3, 4):
+            for flux in (0, 1, 2, 3):
+                yield dict(dim=1, odr=odr, flux=flux, nrk=3, bc=bc)
+
+
+def build_ref_all(jobs: int = 8) -> list:
+    with ThreadPoolExecutor(jobs) as ex:
+        return list(ex.map(lambda kw: build_ref_variant(**kw), all_variants()))
+
+
+if __name__ == "__main__":
+    args = sys.argv[1:] or ["--port"]
+    if "--port" in args:
+        print(build_port(force=True))
+    if "--ref-all" in args:
+        for p in build_ref_all():
+            print(p)

@@ -1,0 +1,842 @@
+/*
+ * CPU oracle for the MLAU per-step hot path.  TEST INFRASTRUCTURE ONLY: it is
+ * the checker that tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline run; the GPU product never links or calls it.
+ *
+ * Restates the reference step drivers (file:line cited per function) in plain
+ * C.  Arithmetic keeps the reference's evaluation order; build with
+ * -O2 -fopenmp -ffp-contract=off (oracle/Makefile), never -ffast-math.
+ * Scratch layout differs from the reference (struct-of-arrays instead of the
+ * reference's stride-8 array-of-structs); the numbers do not.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include "mlau_oracle.h"
+#include "oracle_point.h"
+
+#define IDX3(i, j, k) ((long)nx * ((long)ny * (k) + (j)) + (i))
+
+static double *alloc_d(long n)
+{
+    double *p = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    if (!p) abort();
+    return p;
+}
+
+/* RK coefficients rk_fac (mhd_fd_ct_3d.c:120): U <- a U^n + b (U - dt L(U)). */
+static void rk_coef(int nrk, int stage, double *a, double *b)
+{
+    const double t[3][2] = {{0.0, 1.0},
+                            {0.5 + (nrk - 2) * 0.25, 0.5 - (nrk - 2) * 0.25},
+                            {1. / 3., 2. / 3.}};
+    *a = t[stage][0];
+    *b = t[stage][1];
+}
+
+/* Periodic ghost fill of one 3D array: X, then Y, then Z, each over the full
+ * extent of the other axes (single-rank branch of mpi_sdrv3d,
+ * 3D/MPI/OTvortex/boundary.c:91-104,150-163,209-222). */
+static void fill3d(double *f, int nx, int ny, int nz, int xoff, int yoff, int zoff)
+{
+#pragma omp parallel for
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < xoff; i++) {
+                f[IDX3(nx - 1 - i, j, k)] = f[IDX3(2 * xoff - 1 - i, j, k)];
+                f[IDX3(i, j, k)] = f[IDX3(nx - 2 * xoff + i, j, k)];
+            }
+#pragma omp parallel for
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < yoff; j++)
+            for (int i = 0; i < nx; i++) {
+                f[IDX3(i, ny - 1 - j, k)] = f[IDX3(i, 2 * yoff - 1 - j, k)];
+                f[IDX3(i, j, k)] = f[IDX3(i, ny - 2 * yoff + j, k)];
+            }
+#pragma omp parallel for
+    for (int k = 0; k < zoff; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                f[IDX3(i, j, nz - 1 - k)] = f[IDX3(i, j, 2 * zoff - 1 - k)];
+                f[IDX3(i, j, k)] = f[IDX3(i, j, nz - 2 * zoff + k)];
+            }
+}
+
+/* bc2d periodic branch, 2D/SERIAL/OTvortex/boundary.c:28-57. */
+static void fill2d(double *f, int nx, int ny, int xoff, int yoff)
+{
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < xoff; i++) {
+            f[(long)nx * j + (nx - 1 - i)] = f[(long)nx * j + (2 * xoff - 1 - i)];
+            f[(long)nx * j + i] = f[(long)nx * j + (nx - 2 * xoff + i)];
+        }
+    for (int j = 0; j < yoff; j++)
+        for (int i = 0; i < nx; i++) {
+            f[(long)nx * (ny - 1 - j) + i] = f[(long)nx * (2 * yoff - 1 - j) + i];
+            f[(long)nx * j + i] = f[(long)nx * (ny - 2 * yoff + j) + i];
+        }
+}
+
+/*
+ * One face sweep of the 3D/2D drivers along an axis with element stride `st`
+ * (mhd_fd_ct_3d.c:379-493 for X, :587-701 Y, :795-909 Z; 2D :273-362 and
+ * :404-493).  Variables are passed already rotated to (normal, t, u) order:
+ * vn/vt/vu velocities, cn/ct/cu cell-centred B, bface = face-centred normal B.
+ * dvt/dvu: transverse shock sensors (dvu NULL in 2D).  split_t / split_u
+ * select which tangential B fluxes get the central/upwind split (ql/qr).
+ * Pencils: `npen` lines, line p starts at base[p], with `len` cells along the
+ * axis.  Outputs flux fl[7 arrays] ordered (ro, mn, mt, mu, bt, bu, en) at
+ * face index i (face i-1/2) for i in [3, len-2), and central parts fct/fcu.
+ */
+typedef struct {
+    const double *ro, *vn, *vt, *vu, *cn, *ct, *cu, *pr, *m2, *bface, *dvt, *dvu;
+    int split_t, split_u;
+} sweep_in;
+
+static void sweep_pencil(const sweep_in *S, long base, long st, int len, int odr, int flx,
+                         double gamma, double *const fl[7], double *fct, double *fcu,
+                         double *ul, double *ur, double *qlt, double *qrt, double *qlu,
+                         double *qru)
+{
+    for (int i = 2; i < len - 2; i++) {
+        long c = base + st * i;
+        double q[7][5];
+        for (int m = 0; m < 5; m++) {
+            long s = c + st * (m - 2);
+            q[0][m] = S->ro[s];
+            q[1][m] = S->vn[s];
+            q[2][m] = S->vt[s];
+            q[3][m] = S->vu[s];
+            q[4][m] = S->ct[s];
+            q[5][m] = S->cu[s];
+            q[6][m] = S->pr[s];
+        }
+        double vl[7], vr[7];
+        int full = (o_max(S->m2[c - st], o_max(S->m2[c], S->m2[c + st])) >= 1.0);
+        o_reconst(full, odr, q, S->cn[c], gamma, vl, vr);
+        for (int v = 0; v < 7; v++) {
+            ul[7 * (i + 1) + v] = vl[v];
+            ur[7 * i + v] = vr[v];
+        }
+        double bl = S->bface[c + st], br = S->bface[c];
+        if (S->split_t) {
+            double a5[5], b5[5], la, ra, lb, rb;
+            for (int m = 0; m < 5; m++) {
+                long s = c + st * (m - 2);
+                a5[m] = S->ct[s] * S->vn[s];
+                b5[m] = S->vt[s];
+            }
+            o_lin_lr(odr, a5, &la, &ra);
+            o_lin_lr(odr, b5, &lb, &rb);
+            qlt[i + 1] = la - bl * lb;
+            qrt[i] = ra - br * rb;
+        }
+        if (S->split_u) {
+            double a5[5], b5[5], la, ra, lb, rb;
+            for (int m = 0; m < 5; m++) {
+                long s = c + st * (m - 2);
+                a5[m] = S->cu[s] * S->vn[s];
+                b5[m] = S->vu[s];
+            }
+            o_lin_lr(odr, a5, &la, &ra);
+            o_lin_lr(odr, b5, &lb, &rb);
+            qlu[i + 1] = la - bl * lb;
+            qru[i] = ra - br * rb;
+        }
+    }
+    for (int i = 3; i < len - 2; i++) {
+        long c = base + st * i;
+        double bn = 0.5 * (S->bface[c] + S->bface[c]);
+        double dvtm = S->dvu ? o_min(o_min(S->dvt[c - st], S->dvt[c]),
+                                     o_min(S->dvu[c - st], S->dvu[c]))
+                             : o_min(S->dvt[c - st], S->dvt[c]);
+        double dv[2] = {(S->vn[c] - S->vn[c - st]), dvtm};
+        double f[7];
+        o_flux(flx, &ul[7 * i], &ur[7 * i], bn, gamma, dv, f);
+        for (int v = 0; v < 7; v++) fl[v][c] = f[v];
+        if (S->split_t) {
+            fct[c] = 0.5 * (qlt[i] + qrt[i]);
+            fl[4][c] -= fct[c];
+        }
+        if (S->split_u) {
+            fcu[c] = 0.5 * (qlu[i] + qru[i]);
+            fl[5][c] -= fcu[c];
+        }
+    }
+}
+
+/* Corner (edge) EMF contribution along an axis with stride st: for edge index
+ * j in [3, len-2) of a pencil, ``e += sgn*0.5*((ul0+ur0) + w*(ul1+ur1))`` with
+ * ul/ur the linear face interpolations of the upwind (fu) and central (fc)
+ * parts, w = ct or 1-ct (mhd_fd_ct_3d.c:494-585 and siblings). */
+static void emf_pencil(const double *fu, const double *fc, const double *ctw, int one_minus,
+                       double sgn, double *e, long base, long st, int len, int odr)
+{
+    for (int j = 3; j < len - 2; j++) {
+        long c = base + st * j;
+        double a[5], b[5], ul0, ur0, ul1, ur1, dummy;
+        for (int m = 0; m < 5; m++) {
+            a[m] = fu[c + st * (m - 3)];
+            b[m] = fc[c + st * (m - 3)];
+        }
+        o_lin_lr(odr, a, &ul0, &dummy);
+        o_lin_lr(odr, b, &ul1, &dummy);
+        for (int m = 0; m < 5; m++) {
+            a[m] = fu[c + st * (m - 2)];
+            b[m] = fc[c + st * (m - 2)];
+        }
+        o_lin_lr(odr, a, &dummy, &ur0);
+        o_lin_lr(odr, b, &dummy, &ur1);
+        double w = one_minus ? (1.0 - ctw[c]) : ctw[c];
+        e[c] += sgn * 0.5 * ((ul0 + ur0) + w * (ul1 + ur1));
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3D driver: 3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-1198, one rank, periodic.     */
+/* ------------------------------------------------------------------------ */
+void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                     double *by, double *bz, double dt, double dx, double dy, double dz,
+                     int nx, int ny, int nz, int xoff, int yoff, int zoff, double gamma,
+                     int odr, int flx, int nrk)
+{
+    const long n = (long)nx * ny * nz;
+    const double dtdx = dt / dx, dtdy = dt / dy, dtdz = dt / dz;
+    double *state[8] = {ro, mx, my, mz, bx, by, bz, en};
+    double *u0 = alloc_d(8 * n);
+    for (int v = 0; v < 8; v++) memcpy(u0 + v * n, state[v], sizeof(double) * n);
+
+    double *vx = alloc_d(n), *vy = alloc_d(n), *vz = alloc_d(n), *pr = alloc_d(n);
+    double *cx = alloc_d(n), *cy = alloc_d(n), *cz = alloc_d(n), *m2 = alloc_d(n);
+    double *ex = alloc_d(n), *ey = alloc_d(n), *ez = alloc_d(n);
+    double *ct0 = alloc_d(n), *ct1 = alloc_d(n), *ct2 = alloc_d(n);
+    double *dvx = alloc_d(n), *dvy = alloc_d(n), *dvz = alloc_d(n);
+    double *F[3][7], *FC[3][2];
+    for (int d = 0; d < 3; d++) {
+        for (int v = 0; v < 7; v++) F[d][v] = alloc_d(n);
+        FC[d][0] = alloc_d(n);
+        FC[d][1] = alloc_d(n);
+    }
+    const long sy = nx, sz = (long)nx * ny;
+
+    for (int rk = 0; rk < nrk; rk++) {
+        double ra, rb;
+        rk_coef(nrk, rk, &ra, &rb);
+
+        /* cell-centred B (:186-220) and its periodic fill (:221-238) */
+#pragma omp parallel for
+        for (int k = 0; k < nz; k++) {
+            for (int j = 0; j < ny; j++)
+                for (int i = 1; i < nx - 2; i++) {
+                    long s = IDX3(i, j, k);
+                    cx[s] = o_face2cen(odr, bx[s - 1], bx[s], bx[s + 1], bx[s + 2]);
+                }
+            for (int j = 1; j < ny - 2; j++)
+                for (int i = 0; i < nx; i++) {
+                    long s = IDX3(i, j, k);
+                    cy[s] = o_face2cen(odr, by[s - sy], by[s], by[s + sy], by[s + 2 * sy]);
+                }
+        }
+#pragma omp parallel for
+        for (int k = 1; k < nz - 2; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) {
+                    long s = IDX3(i, j, k);
+                    cz[s] = o_face2cen(odr, bz[s - sz], bz[s], bz[s + sz], bz[s + 2 * sz]);
+                }
+        fill3d(cx, nx, ny, nz, xoff, yoff, zoff);
+        fill3d(cy, nx, ny, nz, xoff, yoff, zoff);
+        fill3d(cz, nx, ny, nz, xoff, yoff, zoff);
+
+        /* primitives (:240-262) */
+#pragma omp parallel for
+        for (long s = 0; s < n; s++) {
+            double iro = 1.0 / ro[s];
+            vx[s] = mx[s] * iro;
+            vy[s] = my[s] * iro;
+            vz[s] = mz[s] * iro;
+            double v2 = (vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
+            double b2 = (cx[s] * cx[s] + cy[s] * cy[s] + cz[s] * cz[s]);
+            pr[s] = (gamma - 1) * (en[s] - 0.5 * (ro[s] * v2 + b2));
+            m2[s] = v2 / (gamma * pr[s] * iro);
+            ex[s] = ey[s] = ez[s] = 0.0;
+            ct0[s] = ct1[s] = ct2[s] = 0.5;
+        }
+
+        /* Alfven-upwind CT weights (:264-340) */
+        const double eps = 1e-6;
+#pragma omp parallel for
+        for (int k = 0; k < nz; k++)
+            for (int j = 1; j < ny; j++)
+                for (int i = 1; i < nx; i++) {
+                    long s = IDX3(i, j, k);
+                    double va = 0.25 * (vx[s - sy - 1] + vx[s - sy] + vx[s - 1] + vx[s]);
+                    double vb = 0.25 * (vy[s - sy - 1] + vy[s - sy] + vy[s - 1] + vy[s]);
+                    double rc = 0.25 * (ro[s - sy - 1] + ro[s - sy] + ro[s - 1] + ro[s]);
+                    rc = 1.0 / sqrt(rc);
+                    double ba = 0.5 * (bx[s - sy] + bx[s]);
+                    double bb = 0.5 * (by[s - 1] + by[s]);
+                    va = fabs(va) + fabs(ba * rc);
+                    vb = fabs(vb) + fabs(bb * rc);
+                    ct0[s] = (va + 0.5 * eps) / (va + vb + eps);
+                }
+#pragma omp parallel for
+        for (int k = 1; k < nz; k++) {
+            for (int j = 1; j < ny; j++)
+                for (int i = 0; i < nx; i++) {
+                    long s = IDX3(i, j, k);
+                    double va = 0.25 * (vy[s - sz - sy] + vy[s - sz] + vy[s - sy] + vy[s]);
+                    double vb = 0.25 * (vz[s - sz - sy] + vz[s - sz] + vz[s - sy] + vz[s]);
+                    double rc = 0.25 * (ro[s - sz - sy] + ro[s - sz] + ro[s - sy] + ro[s]);
+                    rc = 1.0 / sqrt(rc);
+                    double ba = 0.5 * (by[s - sz] + by[s]);
+                    double bb = 0.5 * (bz[s - sy] + bz[s]);
+                    va = fabs(va) + fabs(ba * rc);
+                    vb = fabs(vb) + fabs(bb * rc);
+                    ct1[s] = (va + 0.5 * eps) / (va + vb + eps);
+                }
+            for (int j = 0; j < ny; j++)
+                for (int i = 1; i < nx; i++) {
+                    long s = IDX3(i, j, k);
+                    double va = 0.25 * (vz[s - sz - 1] + vz[s - sz] + vz[s - 1] + vz[s]);
+                    double vb = 0.25 * (vx[s - sz - 1] + vx[s - sz] + vx[s - 1] + vx[s]);
+                    double rc = 0.25 * (ro[s - sz - 1] + ro[s - sz] + ro[s - 1] + ro[s]);
+                    rc = 1.0 / sqrt(rc);
+                    double ba = 0.5 * (bz[s - 1] + bz[s]);
+                    double bb = 0.5 * (bx[s - sz] + bx[s]);
+                    va = fabs(va) + fabs(ba * rc);
+                    vb = fabs(vb) + fabs(bb * rc);
+                    ct2[s] = (va + 0.5 * eps) / (va + vb + eps);
+                }
+        }
+
+        /* shock sensors (:342-377) */
+#pragma omp parallel for
+        for (int k = 1; k < nz - 1; k++)
+            for (int j = 1; j < ny - 1; j++)
+                for (int i = 1; i < nx - 1; i++) {
+                    long s = IDX3(i, j, k);
+                    dvx[s] = o_min((vx[s + 1] - vx[s]), (vx[s] - vx[s - 1]));
+                    dvy[s] = o_min((vy[s + sy] - vy[s]), (vy[s] - vy[s - sy]));
+                    dvz[s] = o_min((vz[s + sz] - vz[s]), (vz[s] - vz[s - sz]));
+                }
+        fill3d(dvx, nx, ny, nz, xoff, yoff, zoff);
+        fill3d(dvy, nx, ny, nz, xoff, yoff, zoff);
+        fill3d(dvz, nx, ny, nz, xoff, yoff, zoff);
+
+        /* three face sweeps; rotated variables (:379-493, :587-701, :795-909) */
+        sweep_in SX = {ro, vx, vy, vz, cx, cy, cz, pr, m2, bx, dvy, dvz, 1, 1};
+        sweep_in SY = {ro, vy, vz, vx, cy, cz, cx, pr, m2, by, dvz, dvx, 1, 1};
+        sweep_in SZ = {ro, vz, vx, vy, cz, cx, cy, pr, m2, bz, dvx, dvy, 1, 1};
+        const sweep_in *SW[3] = {&SX, &SY, &SZ};
+        const int lens[3] = {nx, ny, nz};
+        const long strides[3] = {1, sy, sz};
+        for (int d = 0; d < 3; d++) {
+            int len = lens[d];
+            long st = strides[d];
+            long npen = n / len;
+#pragma omp parallel
+            {
+                double *ul = alloc_d(7 * (len + 1)), *ur = alloc_d(7 * (len + 1));
+                double *q = alloc_d(4 * (len + 1));
+#pragma omp for
+                for (long p = 0; p < npen; p++) {
+                    long base;
+                    if (d == 0) base = p * nx;
+                    else if (d == 1) base = (p / nx) * sz + (p % nx);
+                    else base = p;
+                    sweep_pencil(SW[d], base, st, len, odr, flx, gamma, F[d], FC[d][0],
+                                 FC[d][1], ul, ur, q, q + (len + 1), q + 2 * (len + 1),
+                                 q + 3 * (len + 1));
+                }
+                free(ul);
+                free(ur);
+                free(q);
+            }
+        }
+
+        /* edge EMFs (:494-585, :702-793, :910-1001).  F[d][4] is the flux of
+         * the first tangential B (t), F[d][5] of the second (u):
+         *   X: t=y, u=z;  Y: t=z, u=x;  Z: t=x, u=y. */
+#pragma omp parallel for
+        for (int k = 0; k < nz; k++)
+            for (int i = 3; i < nx - 2; i++)
+                emf_pencil(F[0][4], FC[0][0], ct0, 1, -1.0, ez, IDX3(i, 0, k), sy, ny, odr);
+#pragma omp parallel for
+        for (int j = 0; j < ny; j++)
+            for (int i = 3; i < nx - 2; i++)
+                emf_pencil(F[0][5], FC[0][1], ct2, 0, +1.0, ey, IDX3(i, j, 0), sz, nz, odr);
+#pragma omp parallel for
+        for (int j = 3; j < ny - 2; j++)
+            for (int i = 0; i < nx; i++)
+                emf_pencil(F[1][4], FC[1][0], ct1, 1, -1.0, ex, IDX3(i, j, 0), sz, nz, odr);
+#pragma omp parallel for
+        for (int k = 0; k < nz; k++)
+            for (int j = 3; j < ny - 2; j++)
+                emf_pencil(F[1][5], FC[1][1], ct0, 0, +1.0, ez, IDX3(0, j, k), 1, nx, odr);
+#pragma omp parallel for
+        for (int k = 3; k < nz - 2; k++)
+            for (int j = 0; j < ny; j++)
+                emf_pencil(F[2][4], FC[2][0], ct2, 1, -1.0, ey, IDX3(0, j, k), 1, nx, odr);
+#pragma omp parallel for
+        for (int k = 3; k < nz - 2; k++)
+            for (int i = 0; i < nx; i++)
+                emf_pencil(F[2][5], FC[2][1], ct1, 0, +1.0, ex, IDX3(i, 0, k), sy, ny, odr);
+
+        /* cell-centred update (:1003-1078).  Flux component per direction
+         * for (ro, mx, my, mz, en): X (0,1,2,3,6), Y (0,3,1,2,6), Z (0,2,3,1,6). */
+        static const int cmp[3][5] = {{0, 1, 2, 3, 6}, {0, 3, 1, 2, 6}, {0, 2, 3, 1, 6}};
+        double *cons[5] = {ro, mx, my, mz, en};
+        const int u0v[5] = {0, 1, 2, 3, 7};
+#pragma omp parallel for
+        for (int k = zoff; k < nz - zoff; k++)
+            for (int j = yoff; j < ny - yoff; j++)
+                for (int i = xoff; i < nx - xoff; i++) {
+                    long s = IDX3(i, j, k);
+                    for (int v = 0; v < 5; v++) {
+                        const double *fx = F[0][cmp[0][v]], *fy = F[1][cmp[1][v]],
+                                     *fz = F[2][cmp[2][v]];
+                        double d0 = o_diff(odr, fx[s - 1], fx[s], fx[s + 1], fx[s + 2]);
+                        double d1 = o_diff(odr, fy[s - sy], fy[s], fy[s + sy], fy[s + 2 * sy]);
+                        double d2 = o_diff(odr, fz[s - sz], fz[s], fz[s + sz], fz[s + 2 * sz]);
+                        cons[v][s] = ra * u0[u0v[v] * n + s]
+                                     + rb * (cons[v][s] - dtdx * d0 - dtdy * d1 - dtdz * d2);
+                    }
+                }
+        /* CT update of face B (:1079-1157) */
+#pragma omp parallel for
+        for (int k = zoff; k < nz - zoff; k++) {
+            for (int j = yoff; j < ny - yoff; j++)
+                for (int i = xoff; i < nx - xoff + 1; i++) {
+                    long s = IDX3(i, j, k);
+                    double d0 = o_diff(odr, ez[s - sy], ez[s], ez[s + sy], ez[s + 2 * sy]);
+                    double d1 = o_diff(odr, ey[s - sz], ey[s], ey[s + sz], ey[s + 2 * sz]);
+                    bx[s] = ra * u0[4 * n + s] + rb * (bx[s] - dtdy * d0 + dtdz * d1);
+                }
+            for (int j = yoff; j < ny - yoff + 1; j++)
+                for (int i = xoff; i < nx - xoff; i++) {
+                    long s = IDX3(i, j, k);
+                    double d0 = o_diff(odr, ex[s - sz], ex[s], ex[s + sz], ex[s + 2 * sz]);
+                    double d1 = o_diff(odr, ez[s - 1], ez[s], ez[s + 1], ez[s + 2]);
+                    by[s] = ra * u0[5 * n + s] + rb * (by[s] - dtdz * d0 + dtdx * d1);
+                }
+        }
+#pragma omp parallel for
+        for (int k = zoff; k < nz - zoff + 1; k++)
+            for (int j = yoff; j < ny - yoff; j++)
+                for (int i = xoff; i < nx - xoff; i++) {
+                    long s = IDX3(i, j, k);
+                    double d0 = o_diff(odr, ey[s - 1], ey[s], ey[s + 1], ey[s + 2]);
+                    double d1 = o_diff(odr, ex[s - sy], ex[s], ex[s + sy], ex[s + 2 * sy]);
+                    bz[s] = ra * u0[6 * n + s] + rb * (bz[s] - dtdx * d0 + dtdy * d1);
+                }
+        /* periodic boundary of the 8 conserved arrays (:1161-1175) */
+        for (int v = 0; v < 8; v++) fill3d(state[v], nx, ny, nz, xoff, yoff, zoff);
+    }
+
+    free(u0);
+    double *tmp[] = {vx, vy, vz, pr, cx, cy, cz, m2, ex, ey, ez, ct0, ct1, ct2, dvx, dvy, dvz};
+    for (unsigned t = 0; t < sizeof(tmp) / sizeof(tmp[0]); t++) free(tmp[t]);
+    for (int d = 0; d < 3; d++) {
+        for (int v = 0; v < 7; v++) free(F[d][v]);
+        free(FC[d][0]);
+        free(FC[d][1]);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 2D driver: 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-660, periodic.            */
+/* ------------------------------------------------------------------------ */
+void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                     double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                     int xoff, int yoff, double gamma, int odr, int flx, int nrk)
+{
+    const long n = (long)nx * ny;
+    const double dtdx = dt / dx, dtdy = dt / dy;
+    double *state[8] = {ro, mx, my, mz, bx, by, bz, en};
+    double *u0 = alloc_d(8 * n);
+    for (int v = 0; v < 8; v++) memcpy(u0 + v * n, state[v], sizeof(double) * n);
+    double *vx = alloc_d(n), *vy = alloc_d(n), *vz = alloc_d(n), *pr = alloc_d(n);
+    double *cx = alloc_d(n), *cy = alloc_d(n), *m2 = alloc_d(n), *ez = alloc_d(n);
+    double *ctw = alloc_d(n), *dvx = alloc_d(n), *dvy = alloc_d(n);
+    double *FX[7], *FY[7], *fcx = alloc_d(n), *fcy = alloc_d(n);
+    for (int v = 0; v < 7; v++) { FX[v] = alloc_d(n); FY[v] = alloc_d(n); }
+    const long sy = nx;
+
+    for (int rk = 0; rk < nrk; rk++) {
+        double ra, rb;
+        rk_coef(nrk, rk, &ra, &rb);
+        /* cell-centred B (:172-201) */
+#pragma omp parallel for
+        for (int j = 0; j < ny; j++)
+            for (int i = 1; i < nx - 2; i++) {
+                long s = (long)nx * j + i;
+                cx[s] = o_face2cen(odr, bx[s - 1], bx[s], bx[s + 1], bx[s + 2]);
+            }
+#pragma omp parallel for
+        for (int j = 1; j < ny - 2; j++)
+            for (int i = 0; i < nx; i++) {
+                long s = (long)nx * j + i;
+                cy[s] = o_face2cen(odr, by[s - sy], by[s], by[s + sy], by[s + 2 * sy]);
+            }
+        fill2d(cx, nx, ny, xoff, yoff);
+        fill2d(cy, nx, ny, xoff, yoff);
+        /* primitives (:203-223) */
+#pragma omp parallel for
+        for (long s = 0; s < n; s++) {
+            double iro = 1.0 / ro[s];
+            vx[s] = mx[s] * iro;
+            vy[s] = my[s] * iro;
+            vz[s] = mz[s] * iro;
+            double v2 = (vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
+            double b2 = (cx[s] * cx[s] + cy[s] * cy[s] + bz[s] * bz[s]);
+            pr[s] = (gamma - 1) * (en[s] - 0.5 * (ro[s] * v2 + b2));
+            m2[s] = v2 / (gamma * pr[s] * iro);
+            ez[s] = 0.0;
+            ctw[s] = 0.5;
+        }
+        /* CT weights (:224-249) */
+        const double eps = 1e-6;
+#pragma omp parallel for
+        for (int j = 1; j < ny; j++)
+            for (int i = 1; i < nx; i++) {
+                long s = (long)nx * j + i;
+                double va = 0.25 * (vx[s - sy - 1] + vx[s - sy] + vx[s - 1] + vx[s]);
+                double vb = 0.25 * (vy[s - sy - 1] + vy[s - sy] + vy[s - 1] + vy[s]);
+                double rc = 0.25 * (ro[s - sy - 1] + ro[s - sy] + ro[s - 1] + ro[s]);
+                rc = 1.0 / sqrt(rc);
+                double ba = 0.5 * (bx[s - sy] + bx[s]);
+                double bb = 0.5 * (by[s - 1] + by[s]);
+                va = fabs(va) + fabs(ba * rc);
+                vb = fabs(vb) + fabs(bb * rc);
+                ctw[s] = (va + 0.5 * eps) / (va + vb + eps);
+            }
+        /* shock sensors (:251-271) */
+#pragma omp parallel for
+        for (int j = 1; j < ny - 1; j++)
+            for (int i = 1; i < nx - 1; i++) {
+                long s = (long)nx * j + i;
+                dvx[s] = o_min((vx[s + 1] - vx[s]), (vx[s] - vx[s - 1]));
+                dvy[s] = o_min((vy[s + sy] - vy[s]), (vy[s] - vy[s - sy]));
+            }
+        fill2d(dvx, nx, ny, xoff, yoff);
+        fill2d(dvy, nx, ny, xoff, yoff);
+
+        /* X faces (:273-362): (vn,vt,vu)=(vx,vy,vz), (bt,bu)=(cy,bz); only the
+         * By flux is split.  Y faces (:404-493): (vy,vz,vx), (bz,cx); only Bx. */
+        sweep_in SX = {ro, vx, vy, vz, cx, cy, bz, pr, m2, bx, dvy, NULL, 1, 0};
+        sweep_in SY = {ro, vy, vz, vx, cy, bz, cx, pr, m2, by, dvx, NULL, 0, 1};
+#pragma omp parallel
+        {
+            int L = (nx > ny ? nx : ny) + 1;
+            double *ul = alloc_d(7 * L), *ur = alloc_d(7 * L), *q = alloc_d(4 * L);
+#pragma omp for
+            for (int j = 0; j < ny; j++)
+                sweep_pencil(&SX, (long)nx * j, 1, nx, odr, flx, gamma, FX, fcx, NULL, ul, ur,
+                             q, q + L, q + 2 * L, q + 3 * L);
+#pragma omp for
+            for (int i = 0; i < nx; i++)
+                sweep_pencil(&SY, i, sy, ny, odr, flx, gamma, FY, NULL, fcy, ul, ur, q, q + L,
+                             q + 2 * L, q + 3 * L);
+            free(ul);
+            free(ur);
+            free(q);
+        }
+        /* Ez from x-faces along Y (:364-402) and from y-faces along X (:495-533).
+         * The 2D reference restricts the x-face part to rows j in [3,ny-2) via
+         * its loops; emf_pencil covers the same edges. */
+#pragma omp parallel for
+        for (int i = 3; i < nx - 2; i++)
+            emf_pencil(FX[4], fcx, ctw, 1, -1.0, ez, i, sy, ny, odr);
+#pragma omp parallel for
+        for (int j = 3; j < ny - 2; j++)
+            emf_pencil(FY[5], fcy, ctw, 0, +1.0, ez, (long)nx * j, 1, nx, odr);
+
+        /* cell-centred update incl. Bz (:535-592).  Components per direction
+         * for (ro, mx, my, mz, bz, en): X (0,1,2,3,5,6), Y (0,3,1,2,4,6). */
+        static const int cx2[6] = {0, 1, 2, 3, 5, 6}, cy2[6] = {0, 3, 1, 2, 4, 6};
+        double *cons[6] = {ro, mx, my, mz, bz, en};
+        const int u0v[6] = {0, 1, 2, 3, 6, 7};
+#pragma omp parallel for
+        for (int j = yoff; j < ny - yoff; j++)
+            for (int i = xoff; i < nx - xoff; i++) {
+                long s = (long)nx * j + i;
+                for (int v = 0; v < 6; v++) {
+                    const double *fx = FX[cx2[v]], *fy = FY[cy2[v]];
+                    double d0 = o_diff(odr, fx[s - 1], fx[s], fx[s + 1], fx[s + 2]);
+                    double d1 = o_diff(odr, fy[s - sy], fy[s], fy[s + sy], fy[s + 2 * sy]);
+                    cons[v][s] = ra * u0[u0v[v] * n + s] + rb * (cons[v][s] - dtdx * d0 - dtdy * d1);
+                }
+            }
+        /* CT Bx, By (:593-632) */
+#pragma omp parallel for
+        for (int j = yoff; j < ny - yoff; j++)
+            for (int i = xoff; i < nx - xoff + 1; i++) {
+                long s = (long)nx * j + i;
+                double d = o_diff(odr, ez[s - sy], ez[s], ez[s + sy], ez[s + 2 * sy]);
+                bx[s] = ra * u0[4 * n + s] + rb * (bx[s] - dtdy * d);
+            }
+#pragma omp parallel for
+        for (int j = yoff; j < ny - yoff + 1; j++)
+            for (int i = xoff; i < nx - xoff; i++) {
+                long s = (long)nx * j + i;
+                double d = o_diff(odr, ez[s - 1], ez[s], ez[s + 1], ez[s + 2]);
+                by[s] = ra * u0[5 * n + s] + rb * (by[s] + dtdx * d);
+            }
+        for (int v = 0; v < 8; v++) fill2d(state[v], nx, ny, xoff, yoff);
+    }
+    free(u0);
+    double *tmp[] = {vx, vy, vz, pr, cx, cy, m2, ez, ctw, dvx, dvy, fcx, fcy};
+    for (unsigned t = 0; t < sizeof(tmp) / sizeof(tmp[0]); t++) free(tmp[t]);
+    for (int v = 0; v < 7; v++) { free(FX[v]); free(FY[v]); }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 1D driver: 1D/SERIAL/shock/mhd_fd4c_1d.c:60-271 and the wave variant.     */
+/* ------------------------------------------------------------------------ */
+
+/* openbc1d_mhd, 1D/SERIAL/shock/openbc1d_mhd.c:21-175: characteristic
+ * advection of the boundary data across the domain edge, both sides. */
+static void open_bc_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,
+                       double *bz, double bx, double dx, double dt, int nx, int xoff,
+                       double gamma)
+{
+    const double bx2 = bx * bx, dtdx = dt / dx;
+    for (int side = 0; side <= 1; side++) {
+        int sgn = side ? -1 : 1;
+        int si = side ? (nx - xoff - 1) : xoff;
+        int so = si - sgn;
+        double q[2][7];
+        for (int t = 0; t < 2; t++) {
+            int s = t ? so : si;
+            double r = ro[s], iro = 1.0 / r;
+            double vx = mx[s] * iro, vy = my[s] * iro, vz = mz[s] * iro;
+            double v2 = vx * vx + vy * vy + vz * vz;
+            double b2 = bx * bx + by[s] * by[s] + bz[s] * bz[s];
+            q[t][0] = r;
+            q[t][1] = vx;
+            q[t][2] = vy;
+            q[t][3] = vz;
+            q[t][4] = by[s];
+            q[t][5] = bz[s];
+            q[t][6] = (gamma - 1) * (en[s] - 0.5 * (r * v2 + b2));
+        }
+        double L[7][7], R[7][7], lam[7];
+        o_eigen_full(0.5 * (q[0][0] + q[1][0]), 0.5 * (q[0][1] + q[1][1]),
+                     0.5 * (q[0][2] + q[1][2]), 0.5 * (q[0][3] + q[1][3]), 0.5 * (bx + bx),
+                     0.5 * (q[0][4] + q[1][4]), 0.5 * (q[0][5] + q[1][5]),
+                     0.5 * (q[0][6] + q[1][6]), gamma, lam, L, R);
+        double w[7][2];
+        for (int t = 0; t < 2; t++)
+            for (int m = 0; m < 7; m++)
+                w[m][t] = (+L[m][0] * q[t][0] + L[m][1] * q[t][1] + L[m][2] * q[t][2]
+                           + L[m][3] * q[t][3] + L[m][4] * q[t][4] + L[m][5] * q[t][5]
+                           + L[m][6] * q[t][6]);
+        for (int m = 0; m < 7; m++) {
+            double c = sgn * lam[m];
+            w[m][1] = (c > 0) ? w[m][1] : (1 + c * dtdx) * w[m][1] - c * dtdx * w[m][0];
+        }
+        double p[7];
+        for (int k = 0; k < 7; k++)
+            p[k] = R[0][k] * w[0][1] + R[1][k] * w[1][1] + R[2][k] * w[2][1] + R[3][k] * w[3][1]
+                   + R[4][k] * w[4][1] + R[5][k] * w[5][1] + R[6][k] * w[6][1];
+        ro[so] = p[0];
+        mx[so] = p[1];
+        my[so] = p[2];
+        mz[so] = p[3];
+        by[so] = p[4];
+        bz[so] = p[5];
+        en[so] = p[6];
+        double v2 = mx[so] * mx[so] + my[so] * my[so] + mz[so] * mz[so];
+        double b2 = bx2 + by[so] * by[so] + bz[so] * bz[so];
+        en[so] = en[so] / (gamma - 1.0) + 0.5 * (ro[so] * v2 + b2);
+        mx[so] *= ro[so];
+        my[so] *= ro[so];
+        mz[so] *= ro[so];
+        for (int j = 0; j < xoff - 1; j++) {
+            int s = side * (nx - 1) + sgn * j;
+            ro[s] = ro[so];
+            mx[s] = mx[so];
+            my[s] = my[so];
+            mz[s] = mz[so];
+            by[s] = by[so];
+            bz[s] = bz[so];
+            en[s] = en[so];
+        }
+    }
+}
+
+static void fill1d(double *f, int nx, int xoff)
+{
+    for (int i = 0; i < xoff; i++) {
+        f[nx - 1 - i] = f[2 * xoff - 1 - i];
+        f[i] = f[nx - 2 * xoff + i];
+    }
+}
+
+void oracle_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,
+                    double *bz, double bx, double dt, double dx, int nx, int xoff, double gamma,
+                    int odr, int flx, int nrk, int bc)
+{
+    const double dtdx = dt / dx, bx2 = bx * bx;
+    double *state[7] = {ro, mx, my, mz, by, bz, en};
+    double *u0 = alloc_d(7L * nx);
+    for (int v = 0; v < 7; v++) memcpy(u0 + (long)v * nx, state[v], sizeof(double) * nx);
+    double *vx = alloc_d(nx), *vy = alloc_d(nx), *vz = alloc_d(nx), *pr = alloc_d(nx);
+    double *ul = alloc_d(7L * (nx + 1)), *ur = alloc_d(7L * (nx + 1)), *fx = alloc_d(7L * nx);
+
+    for (int rk = 0; rk < nrk; rk++) {
+        double ra, rb;
+        rk_coef(nrk, rk, &ra, &rb);
+        for (int i = 0; i < nx; i++) {
+            double iro = 1.0 / ro[i];
+            vx[i] = mx[i] * iro;
+            vy[i] = my[i] * iro;
+            vz[i] = mz[i] * iro;
+            double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+            double b2 = bx2 + by[i] * by[i] + bz[i] * bz[i];
+            pr[i] = (gamma - 1) * (en[i] - 0.5 * (ro[i] * v2 + b2));
+        }
+        /* faces (:133-186); full eigen-system where any of the three central
+         * cells is sonic-supersonic */
+        for (int i = 2; i < nx - 2; i++) {
+            double q[7][5];
+            for (int m = 0; m < 5; m++) {
+                int s = i + m - 2;
+                q[0][m] = ro[s];
+                q[1][m] = vx[s];
+                q[2][m] = vy[s];
+                q[3][m] = vz[s];
+                q[4][m] = by[s];
+                q[5][m] = bz[s];
+                q[6][m] = pr[s];
+            }
+            double mach[3];
+            for (int t = 0; t < 3; t++) {
+                double c2 = gamma * q[6][1 + t] / q[0][1 + t];
+                double v2 = q[1][1 + t] * q[1][1 + t] + q[2][1 + t] * q[2][1 + t]
+                            + q[3][1 + t] * q[3][1 + t];
+                mach[t] = v2 / c2;
+            }
+            int full = (o_max(mach[0], o_max(mach[1], mach[2])) >= 1.0);
+            double vl[7], vr[7];
+            o_reconst(full, odr, q, bx, gamma, vl, vr);
+            for (int v = 0; v < 7; v++) {
+                ul[7 * (i + 1) + v] = vl[v];
+                ur[7 * i + v] = vr[v];
+            }
+        }
+        for (int i = 3; i < nx - 2; i++) {
+            double dv[2] = {(vx[i] - vx[i - 1]), 0.0};
+            o_flux(flx, &ul[7 * i], &ur[7 * i], bx, gamma, dv, &fx[7 * i]);
+        }
+        if (bc == ORACLE_BC1D_OPEN && rk == 0)
+            open_bc_1d(ro, mx, my, mz, en, by, bz, bx, dx, dt, nx, xoff, gamma);
+        /* update (:220-255): flux order (ro, mx, my, mz, by, bz, en) */
+        for (int i = 4; i < nx - 4; i++)
+            for (int v = 0; v < 7; v++) {
+                double d = o_diff(odr, fx[7 * (i - 1) + v], fx[7 * i + v], fx[7 * (i + 1) + v],
+                                  fx[7 * (i + 2) + v]);
+                state[v][i] = ra * u0[(long)v * nx + i] + rb * (state[v][i] - dtdx * d);
+            }
+        if (bc == ORACLE_BC1D_PERIODIC)
+            for (int v = 0; v < 7; v++) fill1d(state[v], nx, xoff);
+    }
+    free(u0);
+    free(vx);
+    free(vy);
+    free(vz);
+    free(pr);
+    free(ul);
+    free(ur);
+    free(fx);
+}
+
+/* ------------------------------------------------------------------------ */
+/* CFL dt                                                                    */
+/* ------------------------------------------------------------------------ */
+double oracle_cfl_3d(const double *ro, const double *mx, const double *my, const double *mz,
+                     const double *en, const double *bx, const double *by, const double *bz,
+                     int nx, int ny, int nz, int xoff, int yoff, int zoff, double gamma,
+                     double cfl, double dr, double vfast, double dt_old, double *vmax_out)
+{
+    double vmax = vfast;
+    for (int k = zoff; k < nz - zoff; k++)
+        for (int j = yoff; j < ny - yoff; j++)
+            for (int i = xoff; i < nx - xoff; i++) {
+                long s = IDX3(i, j, k);
+                double iro = 1.0 / ro[s];
+                double vx = mx[s] * iro, vy = my[s] * iro, vz = mz[s] * iro;
+                double bxc = 0.5 * (bx[s] + bx[s + 1]);
+                double byc = 0.5 * (by[s] + by[s + nx]);
+                double bzc = 0.5 * (bz[s] + bz[s + (long)nx * ny]);
+                double v2 = vx * vx + vy * vy + vz * vz;
+                double b2 = bxc * bxc + byc * byc + bzc * bzc;
+                double p = (gamma - 1) * (en[s] - 0.5 * (ro[s] * v2 + b2));
+                double cf = sqrt((0.5 * gamma * (2.0 * p) + b2) / (ro[s]));
+                double vt = sqrt(v2) + cf;
+                if (vt > vmax) vmax = vt;
+            }
+    if (vmax_out) *vmax_out = vmax;
+    return isfinite(vmax) ? cfl * dr / vmax : dt_old;
+}
+
+double oracle_cfl_2d(const double *ro, const double *mx, const double *my, const double *mz,
+                     const double *en, const double *bx, const double *by, const double *bz,
+                     int nx, int ny, int xoff, int yoff, double gamma, double cfl, double dr,
+                     double vfast, double dt_old, double *vmax_out)
+{
+    double vmax = vfast;
+    for (int j = yoff; j < ny - yoff; j++)
+        for (int i = xoff; i < nx - xoff; i++) {
+            long s = (long)nx * j + i;
+            double iro = 1.0 / ro[s];
+            double vx = mx[s] * iro, vy = my[s] * iro, vz = mz[s] * iro;
+            double bxc = 0.5 * (bx[s] + bx[s + 1]);
+            double byc = 0.5 * (by[s] + by[s + nx]);
+            double bzc = bz[s];
+            double v2 = vx * vx + vy * vy + vz * vz;
+            double b2 = bxc * bxc + byc * byc + bzc * bzc;
+            double p = (gamma - 1) * (en[s] - 0.5 * (ro[s] * v2 + b2));
+            double cf = sqrt((0.5 * gamma * (2.0 * p) + b2) / (ro[s]));
+            double vt = sqrt(vx * vx + vy * vy) + cf;
+            if (vt > vmax) vmax = vt;
+        }
+    if (vmax_out) *vmax_out = vmax;
+    return isfinite(vmax) ? cfl * dr / vmax : dt_old;
+}
+
+double oracle_dt_1d(const double *ro, const double *mx, const double *my, const double *mz,
+                    const double *en, const double *by, const double *bz, double bx, int nx,
+                    double gamma, double cfl, double dx, double vfloor)
+{
+    double vmax = vfloor;
+    for (int i = 0; i < nx; i++) {
+        double iro = 1.0 / ro[i];
+        double vx = mx[i] * iro, vy = my[i] * iro, vz = mz[i] * iro;
+        double v2 = vx * vx + vy * vy + vz * vz;
+        double b2 = bx * bx + by[i] * by[i] + bz[i] * bz[i];
+        double p = (gamma - 1) * (en[i] - 0.5 * (ro[i] * v2 + b2));
+        double cf = sqrt((gamma * p + b2) * iro);
+        double vt = fabs(vx) + cf;
+        if (vt > vmax) vmax = vt;
+    }
+    return cfl * dx / vmax;
+}
+
+/* ------------------------------------------------------------------------ */
+void oracle_rec_lr(int odr, const double *f5, double *fl, double *fr) { o_rec_lr(odr, f5, fl, fr); }
+
+void oracle_flux(int flx, const double *in, const double *dv, double *out)
+{
+    o_flux(flx, in, in + 7, in[14], in[15], dv, out);
+}
+
+void oracle_reconst(int full, int odr, const double *prim35, double bn, double gamma,
+                    double *ul, double *ur)
+{
+    double q[7][5];
+    for (int k = 0; k < 7; k++)
+        for (int m = 0; m < 5; m++) q[k][m] = prim35[5 * k + m];
+    o_reconst(full, odr, q, bn, gamma, ul, ur);
+}
