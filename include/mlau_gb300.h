@@ -1,0 +1,155 @@
+/*
+ * mlau_gb300.h - C ABI of the GB300 (sm_103a) MHD step library
+ * (libmlau_gb300.so).
+ *
+ * Two layers:
+ *
+ * 1. Drop-in step drivers with the reference solver's names and parameter
+ *    lists.  Each call copies the caller's host arrays to the GPU, advances
+ *    one full SSP-RK step there, and copies them back, in place, like the
+ *    reference's OpenMP drivers.  The library exports each one twice: with C
+ *    linkage (the names below) and with the reference's own C++ linkage, so
+ *    that an unmodified problem main.cpp relinks against this library in
+ *    place of the driver object file.
+ *
+ * 2. A handle API that keeps a simulation resident in HBM across steps (the
+ *    fast path): create / upload / step / cfl / download / destroy.
+ *
+ * Arrays: one float64 array per variable, x fastest, index nx*(ny*k+j)+i,
+ * ghost cells included (the reference layout).  Face-centred bx[i] sits at
+ * x_{i-1/2}, by[j] at y_{j-1/2}, bz[k] at z_{k-1/2}.  Boundaries: periodic.
+ *
+ * Errors: status-returning calls return 0 on success and a negative MLAU_ERR_*
+ * code otherwise; mlau_last_error() gives the message.  The void drop-in
+ * drivers keep the reference's void signature; on error they leave the
+ * arrays untouched, print the message to stderr and record it.
+ */
+#ifndef MLAU_GB300_H
+#define MLAU_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MLAU_OK = 0,
+    MLAU_ERR_ARG = -1,         /* invalid argument or unsupported configuration */
+    MLAU_ERR_CUDA = -2,        /* CUDA runtime error */
+    MLAU_ERR_NOMEM = -3,       /* device memory exhausted / over budget */
+    MLAU_ERR_STATE = -4,       /* NaN or non-positive density/pressure seen */
+    MLAU_ERR_TIMEOUT = -5      /* a bounded device-side wait gave up */
+};
+
+/* Riemann solvers of include/mhd_flux.h. */
+enum { MLAU_FLUX_MLAU = 0, MLAU_FLUX_LHLLD = 1, MLAU_FLUX_HLLD = 2, MLAU_FLUX_ROE = 3 };
+/* Arithmetic of the reconstruction and Riemann solver. */
+enum { MLAU_FP64 = 0, MLAU_FP32_SPLIT = 1 };
+/* 1D boundaries. */
+enum { MLAU_BC1D_OPEN = 0, MLAU_BC1D_PERIODIC = 1 };
+
+/* ---------------------------------------------------------------------- */
+/* 1. Drop-in drivers                                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces mhd_fd_ct_3d (3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-103, prototype
+ * 3D/MPI/OTvortex/myfunc.h:48-52, caller 3D/MPI/OTvortex/main.cpp:48-50).
+ * Single GPU: mpi_numx = mpi_numy = mpi_numz = 1 and mpi_rank = 0 are
+ * required. */
+void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                  double *by, double *bz, double dt, double dx, double dy, double dz, int nx,
+                  int ny, int nz, int xoff, int yoff, int zoff, double gamma, int mpi_rank,
+                  int mpi_numx, int mpi_numy, int mpi_numz);
+
+/* Replaces the serial mhd_fd_ct_2d (2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-94,
+ * caller 2D/SERIAL/OTvortex/main.cpp:30-31). */
+void mhd_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                  double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                  int xoff, int yoff, double gamma);
+
+/* Replaces the MPI form of mhd_fd_ct_2d (2D/MPI/OTvortex/mhd_fd_ct_2d.c:95-99,
+ * caller 2D/MPI/OTvortex/main.cpp:48-50); C++ callers reach it under the
+ * reference's overloaded name.  mpi_numx = mpi_numy = 1 required. */
+void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                      double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                      int xoff, int yoff, double gamma, int mpi_rank, int mpi_numx,
+                      int mpi_numy);
+
+/* Replaces mhd_fd4c_1d (1D/SERIAL/shock/mhd_fd4c_1d.c:60-63, caller
+ * 1D/SERIAL/shock/main.cpp:166-167).  Boundary: mlau_set_bc_1d (default
+ * open, as the shock driver; periodic as 1D/SERIAL/wave). */
+void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,
+                 double *bz, double bx, double dt, double dx, int nx, int xoff, double gamma);
+
+/* The reference fixes the spatial order (ODR), Runge-Kutta order (R_K) and
+ * Riemann solver (func_flux=) at compile time in each driver copy
+ * (mhd_fd_ct_3d.c:25-27,131-138).  The drop-in drivers read them from here
+ * (dim = 1, 2 or 3).  Defaults are those of the shipped driver files:
+ * 3D and 2D odr=2, nrk=3, LHLLD; 1D odr=1, nrk=2, LHLLD.  The environment
+ * variables MLAU_ODR, MLAU_RK and MLAU_FLUX (mlau|lhlld|hlld|roe) override
+ * the defaults at first use. */
+int mlau_set_scheme(int dim, int odr, int flux, int nrk);
+int mlau_set_bc_1d(int bc);
+const char *mlau_last_error(void);
+void mlau_clear_error(void);
+
+/* ---------------------------------------------------------------------- */
+/* 2. Device-resident handle API                                           */
+/* ---------------------------------------------------------------------- */
+typedef struct mlau_sim mlau_sim;
+
+/* dim 3: nx,ny,nz padded sizes; dim 2: nz = 1; dim 1: ny = nz = 1.
+ * xoff/yoff/zoff: ghost depth (>= 3; the reference uses 4).  Interior width
+ * must be at least the ghost depth.  odr 1..4, flux MLAU_FLUX_*, nrk 1..3,
+ * precision MLAU_FP64 or MLAU_FP32_SPLIT (3D only). */
+int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, int yoff,
+                    int zoff, double dx, double dy, double dz, double gamma, int odr, int flux,
+                    int nrk, int precision);
+int mlau_sim_destroy(mlau_sim *sim);
+/* Host arrays in the order (ro, mx, my, mz, en, bx, by, bz); in 1D bx is
+ * unused (set it with mlau_sim_set_bx_1d). */
+int mlau_sim_upload(mlau_sim *sim, const double *const *host8);
+int mlau_sim_download(mlau_sim *sim, double *const *host8);
+int mlau_sim_set_bx_1d(mlau_sim *sim, double bx);
+int mlau_sim_set_bc_1d(mlau_sim *sim, int bc);
+/* nsteps full RK steps with fixed dt, enqueued on the simulation's stream. */
+int mlau_sim_step(mlau_sim *sim, double dt, int nsteps);
+/* CFL time step (3D/MPI/OTvortex/cflcheck.hpp:1-39, 2D cflcheck.hpp,
+ * 1D/SERIAL/shock/main.cpp:113-128): dt = cfl*dr/max(vfast, max fast speed),
+ * dt_old kept when that maximum is not finite.  Synchronizes the stream. */
+int mlau_sim_cfl(mlau_sim *sim, double cfl, double dr, double vfast, double dt_old,
+                 double *dt_out, double *vmax_out);
+int mlau_sim_sync(mlau_sim *sim);
+/* cudaStream_t of the simulation, for callers that time or order work. */
+void *mlau_sim_stream(mlau_sim *sim);
+/* Device pointer of variable v (same order as upload). */
+int mlau_sim_device_ptr(mlau_sim *sim, int v, double **ptr);
+/* Per-kernel CUDA-event timing (off by default).  kind: 0 prim, 1 aux,
+ * 2 reconstruction, 3 flux, 4 emf, 5 update, 6 copy, 7 cfl, 8 split sweep,
+ * 9 split prep, 10 split update. */
+int mlau_sim_set_timing(mlau_sim *sim, int on);
+int mlau_sim_timing(mlau_sim *sim, int kind, long *count, double *total_ms);
+/* Device bytes held by the simulation. */
+long long mlau_sim_device_bytes(mlau_sim *sim);
+/* Number of kernel launches one mlau_sim_step(sim, dt, 1) issues. */
+int mlau_sim_launches_per_step(mlau_sim *sim);
+/* Enqueue nsteps steps between two CUDA events recorded on the simulation's
+ * stream and return the elapsed device time in milliseconds. */
+int mlau_sim_time_steps(mlau_sim *sim, double dt, int nsteps, double *ms);
+
+/* ---------------------------------------------------------------------- */
+/* 3. Measurement helpers                                                  */
+/* ---------------------------------------------------------------------- */
+/* FMA throughput of the current device in flop/s (2 flops per FMA), FP64 and
+ * FP32: the pipe rates that bound the plain and the split step. */
+int mlau_measure_fma_peaks(double *fp64_flops, double *fp32_flops);
+/* Page-lock (pin) / release caller-owned host memory, so that the drop-in
+ * drivers' host<->device copies run at full link speed. */
+int mlau_pin_host(void *ptr, long long bytes);
+int mlau_unpin_host(void *ptr);
+/* Select the CUDA device used by this host thread's later calls. */
+int mlau_set_device(int device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

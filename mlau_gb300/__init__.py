@@ -1,0 +1,289 @@
+"""GB300-native (sm_103a) MHD step library: Python binding of libmlau_gb300.so.
+
+The compute path is the CUDA library built in-tree by ``mlau_gb300._build``;
+this module only binds its C ABI (include/mlau_gb300.h) with ctypes.  There is
+no CPU fallback: if the library is missing, loading raises.
+
+Two call styles, as in the C ABI:
+
+* reference-style drivers that update numpy arrays in place, with the
+  reference's argument lists: ``mhd_fd_ct_3d``, ``mhd_fd_ct_2d``,
+  ``mhd_fd4c_1d`` (each call: host -> GPU, one RK step, GPU -> host);
+* ``Sim``, a device-resident simulation handle for the fast path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmlau_gb300.so")
+
+FLUX = {"mlau": 0, "lhlld": 1, "hlld": 2, "roe": 3}
+FP64, FP32_SPLIT = 0, 1
+BC1D = {"open": 0, "periodic": 1}
+VARS = ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")
+KERNEL_KINDS = ("prim", "aux", "rec", "flux", "emf", "update", "copy", "cfl",
+                "split_sweep", "split_prep", "split_update")
+
+
+class MlauError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def _bind(lib):
+    d, i, vp = C.c_double, C.c_int, C.c_void_p
+    pd = C.POINTER(C.c_double)
+    lib.mlau_last_error.restype = C.c_char_p
+    lib.mlau_clear_error.restype = None
+    lib.mlau_sim_create.argtypes = [C.POINTER(vp), i, i, i, i, i, i, i, d, d, d, d, i, i, i, i]
+    lib.mlau_sim_destroy.argtypes = [vp]
+    lib.mlau_sim_upload.argtypes = [vp, C.POINTER(pd)]
+    lib.mlau_sim_download.argtypes = [vp, C.POINTER(pd)]
+    lib.mlau_sim_set_bx_1d.argtypes = [vp, d]
+    lib.mlau_sim_set_bc_1d.argtypes = [vp, i]
+    lib.mlau_sim_step.argtypes = [vp, d, i]
+    lib.mlau_sim_cfl.argtypes = [vp, d, d, d, d, pd, pd]
+    lib.mlau_sim_sync.argtypes = [vp]
+    lib.mlau_sim_stream.argtypes = [vp]
+    lib.mlau_sim_stream.restype = vp
+    lib.mlau_sim_device_ptr.argtypes = [vp, i, C.POINTER(pd)]
+    lib.mlau_sim_set_timing.argtypes = [vp, i]
+    lib.mlau_sim_timing.argtypes = [vp, i, C.POINTER(C.c_long), pd]
+    lib.mlau_sim_device_bytes.argtypes = [vp]
+    lib.mlau_sim_device_bytes.restype = C.c_longlong
+    lib.mlau_sim_launches_per_step.argtypes = [vp]
+    lib.mlau_sim_time_steps.argtypes = [vp, d, i, pd]
+    lib.mlau_measure_fma_peaks.argtypes = [pd, pd]
+    lib.mlau_pin_host.argtypes = [vp, C.c_longlong]
+    lib.mlau_unpin_host.argtypes = [vp]
+    lib.mlau_set_device.argtypes = [i]
+    lib.mlau_set_scheme.argtypes = [i, i, i, i]
+    lib.mlau_set_bc_1d.argtypes = [i]
+    lib.mhd_fd_ct_3d.argtypes = [pd] * 8 + [d] * 4 + [i] * 6 + [d] + [i] * 4
+    lib.mhd_fd_ct_3d.restype = None
+    lib.mhd_fd_ct_2d.argtypes = [pd] * 8 + [d] * 3 + [i] * 4 + [d]
+    lib.mhd_fd_ct_2d.restype = None
+    lib.mhd_fd4c_1d.argtypes = [pd] * 7 + [d] * 3 + [i, i, d]
+    lib.mhd_fd4c_1d.restype = None
+    return lib
+
+
+def lib():
+    """The loaded library; raises MlauError when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MlauError(f"{LIB_PATH} is missing: build it with "
+                            "`python -c 'import __graft_entry__ as g; g.build()'`")
+        _lib = _bind(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def last_error() -> str:
+    return lib().mlau_last_error().decode(errors="replace")
+
+
+def _check(rc):
+    if rc != 0:
+        raise MlauError(f"mlau error {rc}: {last_error()}")
+
+
+def _ptr(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise MlauError("arrays must be C-contiguous float64")
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _flux(f):
+    return FLUX[f] if isinstance(f, str) else int(f)
+
+
+# --- reference-style drivers --------------------------------------------------
+def set_scheme(dim: int, odr: int, flux="lhlld", nrk: int = 3):
+    _check(lib().mlau_set_scheme(dim, odr, _flux(flux), nrk))
+
+
+def set_bc_1d(bc: str):
+    _check(lib().mlau_set_bc_1d(BC1D[bc]))
+
+
+def mhd_fd_ct_3d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, dz, nx, ny, nz, xoff, yoff, zoff,
+                 gamma, mpi_rank=0, mpi_numx=1, mpi_numy=1, mpi_numz=1):
+    """Reference 3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-103 signature; in place."""
+    before = _clear()
+    lib().mhd_fd_ct_3d(*[_ptr(a) for a in (ro, mx, my, mz, en, bx, by, bz)], dt, dx, dy, dz, nx, ny,
+                   nz, xoff, yoff, zoff, gamma, mpi_rank, mpi_numx, mpi_numy, mpi_numz)
+    _raise_if_new(before)
+
+
+def mhd_fd_ct_2d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma):
+    """Reference 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-94 signature; in place."""
+    before = _clear()
+    lib().mhd_fd_ct_2d(*[_ptr(a) for a in (ro, mx, my, mz, en, bx, by, bz)], dt, dx, dy, nx, ny,
+                       xoff, yoff, gamma)
+    _raise_if_new(before)
+
+
+def mhd_fd4c_1d(ro, mx, my, mz, en, by, bz, bx, dt, dx, nx, xoff, gamma):
+    """Reference 1D/SERIAL/shock/mhd_fd4c_1d.c:60-63 signature; in place."""
+    before = _clear()
+    lib().mhd_fd4c_1d(*[_ptr(a) for a in (ro, mx, my, mz, en, by, bz)], bx, dt, dx, nx, xoff,
+                      gamma)
+    _raise_if_new(before)
+
+
+def _clear():
+    lib().mlau_clear_error()
+    return ""
+
+
+def _raise_if_new(before):
+    # The void drivers report failures through mlau_last_error(), which is
+    # cleared before each call.
+    after = last_error()
+    if after and after != before:
+        raise MlauError(after)
+
+
+def measure_fma_peaks():
+    """(FP64, FP32) FMA throughput of the current GPU in flop/s."""
+    a, b = C.c_double(), C.c_double()
+    _check(lib().mlau_measure_fma_peaks(C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def set_device(dev: int):
+    _check(lib().mlau_set_device(dev))
+
+
+def pin(arr: np.ndarray):
+    _check(lib().mlau_pin_host(arr.ctypes.data, arr.nbytes))
+
+
+def unpin(arr: np.ndarray):
+    _check(lib().mlau_unpin_host(arr.ctypes.data))
+
+
+# --- device-resident handle ---------------------------------------------------
+class Sim:
+    """A simulation resident on the GPU (handle API of include/mlau_gb300.h)."""
+
+    def __init__(self, dim, shape, off=4, dx=1.0, dy=1.0, dz=1.0, gamma=5 / 3, odr=4,
+                 flux="mlau", nrk=3, precision=FP64):
+        shape = tuple(shape)
+        if dim == 3:
+            nz, ny, nx = shape
+        elif dim == 2:
+            (ny, nx), nz = shape, 1
+        else:
+            (nx,), ny, nz = shape, 1, 1
+        self.dim, self.shape = dim, shape
+        h = C.c_void_p()
+        _check(lib().mlau_sim_create(C.byref(h), dim, nx, ny, nz, off, off if dim >= 2 else 0,
+                                     off if dim == 3 else 0, dx, dy, dz, gamma, odr, _flux(flux),
+                                     nrk, precision))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mlau_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _vars(self):
+        return VARS if self.dim != 1 else ("ro", "mx", "my", "mz", "en", None, "by", "bz")
+
+    def upload(self, state: dict):
+        ptrs = (C.POINTER(C.c_double) * 8)()
+        keep = []
+        for v, k in enumerate(self._vars()):
+            if k is None:
+                continue
+            a = np.ascontiguousarray(state[k], dtype=np.float64)
+            if a.shape != self.shape:
+                raise MlauError(f"{k}: shape {a.shape} != {self.shape}")
+            keep.append(a)
+            ptrs[v] = _ptr(a)
+        _check(lib().mlau_sim_upload(self._h, ptrs))
+        _check(lib().mlau_sim_sync(self._h))
+
+    def download(self, out: dict | None = None) -> dict:
+        out = out if out is not None else {}
+        ptrs = (C.POINTER(C.c_double) * 8)()
+        for v, k in enumerate(self._vars()):
+            if k is None:
+                continue
+            if k not in out:
+                out[k] = np.empty(self.shape, dtype=np.float64)
+            ptrs[v] = _ptr(out[k])
+        _check(lib().mlau_sim_download(self._h, ptrs))
+        return out
+
+    def set_bx(self, bx: float):
+        _check(lib().mlau_sim_set_bx_1d(self._h, bx))
+
+    def set_bc(self, bc: str):
+        _check(lib().mlau_sim_set_bc_1d(self._h, BC1D[bc]))
+
+    def step(self, dt: float, nsteps: int = 1):
+        _check(lib().mlau_sim_step(self._h, dt, nsteps))
+
+    def sync(self):
+        _check(lib().mlau_sim_sync(self._h))
+
+    def cfl(self, cfl, dr, vfast, dt_old=0.0):
+        dt, vm = C.c_double(), C.c_double()
+        _check(lib().mlau_sim_cfl(self._h, cfl, dr, vfast, dt_old, C.byref(dt), C.byref(vm)))
+        return dt.value, vm.value
+
+    @property
+    def stream(self) -> int:
+        return lib().mlau_sim_stream(self._h) or 0
+
+    def device_ptr(self, var: str) -> int:
+        p = C.POINTER(C.c_double)()
+        _check(lib().mlau_sim_device_ptr(self._h, VARS.index(var), C.byref(p)))
+        return C.cast(p, C.c_void_p).value
+
+    def set_timing(self, on: bool):
+        _check(lib().mlau_sim_set_timing(self._h, int(on)))
+
+    def timing(self) -> dict:
+        out = {}
+        for k, name in enumerate(KERNEL_KINDS):
+            n, ms = C.c_long(), C.c_double()
+            _check(lib().mlau_sim_timing(self._h, k, C.byref(n), C.byref(ms)))
+            if n.value:
+                out[name] = (n.value, ms.value)
+        return out
+
+    def time_steps(self, dt: float, nsteps: int) -> float:
+        """Device time (ms) of nsteps steps, CUDA events on the simulation's stream."""
+        ms = C.c_double()
+        _check(lib().mlau_sim_time_steps(self._h, dt, nsteps, C.byref(ms)))
+        return ms.value
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().mlau_sim_device_bytes(self._h))
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(lib().mlau_sim_launches_per_step(self._h))

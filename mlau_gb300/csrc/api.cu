@@ -1,0 +1,517 @@
+// C ABI of the library: the handle API and the reference-named drop-in
+// drivers (declared in include/mlau_gb300.h).
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "sim.cuh"
+
+namespace mlau {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int dalloc(Sim *s, double **p, long long count)
+{
+    void *q = nullptr;
+    size_t bytes = sizeof(double) * (size_t)(count > 0 ? count : 1);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        *p = nullptr;
+        return 1;
+    }
+    s->allocs.push_back(q);
+    s->bytes += (long long)bytes;
+    *p = (double *)q;
+    return 0;
+}
+
+// --- per-kernel event timing ------------------------------------------------
+cudaEvent_t KernelTimer::ev()
+{
+    if (used == pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        pool.push_back(e);
+    }
+    return pool[used++];
+}
+void KernelTimer::begin(int, cudaEvent_t &a)
+{
+    a = ev();
+    cudaEventRecord(a, stream);
+}
+void KernelTimer::end(int kind, cudaEvent_t a)
+{
+    cudaEvent_t b = ev();
+    cudaEventRecord(b, stream);
+    recs.push_back({kind, a, b});
+    if (recs.size() > 4096) flush();
+}
+int KernelTimer::flush()
+{
+    if (recs.empty()) return MLAU_OK;
+    MLAU_CUDA(cudaEventSynchronize(recs.back().b));
+    for (auto &r : recs) {
+        float ms = 0.f;
+        MLAU_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        total_ms[r.kind] += ms;
+        count[r.kind] += 1;
+    }
+    recs.clear();
+    used = 0;
+    return MLAU_OK;
+}
+void KernelTimer::reset()
+{
+    flush();
+    for (int k = 0; k < KK_COUNT; k++) { total_ms[k] = 0; count[k] = 0; }
+}
+KernelTimer::~KernelTimer()
+{
+    for (auto e : pool) cudaEventDestroy(e);
+}
+
+static int check_geometry(int dim, int nx, int ny, int nz, int ox, int oy, int oz)
+{
+    auto ok_axis = [](int n, int off) { return off >= 3 && n - 2 * off >= off; };
+    if (dim < 1 || dim > 3) { set_error("dim must be 1, 2 or 3 (got %d)", dim); return 0; }
+    if (!ok_axis(nx, ox)) {
+        set_error("x: need ghost depth >= 3 and interior width >= ghost depth (nx=%d, off=%d)", nx, ox);
+        return 0;
+    }
+    if (dim >= 2 && !ok_axis(ny, oy)) {
+        set_error("y: need ghost depth >= 3 and interior width >= ghost depth (ny=%d, off=%d)", ny, oy);
+        return 0;
+    }
+    if (dim == 3 && !ok_axis(nz, oz)) {
+        set_error("z: need ghost depth >= 3 and interior width >= ghost depth (nz=%d, off=%d)", nz, oz);
+        return 0;
+    }
+    if ((double)nx * ny * nz > 2.0e9) { set_error("grid too large for 32-bit cell indices"); return 0; }
+    return 1;
+}
+
+int launches_per_step(const Sim *s)
+{
+    if (s->precision == MLAU_FP32_SPLIT) return 1 + 3 * s->nrk + 0;  // refined in split3d
+    if (s->g.dim == 3) return s->nrk * 10;
+    if (s->g.dim == 2) return s->nrk * 8;
+    return s->nrk * 4;
+}
+
+}  // namespace mlau
+
+using namespace mlau;
+
+struct mlau_sim : public Sim {};
+
+extern "C" {
+
+const char *mlau_last_error(void) { return g_err; }
+
+void mlau_clear_error(void) { g_err[0] = 0; }
+
+int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, int yoff,
+                    int zoff, double dx, double dy, double dz, double gamma, int odr, int flux,
+                    int nrk, int precision)
+{
+    if (!out) { set_error("null output pointer"); return MLAU_ERR_ARG; }
+    *out = nullptr;
+    if (dim == 1) { ny = nz = 1; yoff = zoff = 0; }
+    if (dim == 2) { nz = 1; zoff = 0; }
+    if (!check_geometry(dim, nx, ny, nz, xoff, yoff, zoff)) return MLAU_ERR_ARG;
+    if (odr < 1 || odr > 4 || flux < 0 || flux > 3 || nrk < 1 || nrk > 3) {
+        set_error("scheme out of range (odr 1..4, flux 0..3, nrk 1..3)");
+        return MLAU_ERR_ARG;
+    }
+    if (precision != MLAU_FP64 && !(precision == MLAU_FP32_SPLIT && dim == 3)) {
+        set_error("precision %d not available for dim %d", precision, dim);
+        return MLAU_ERR_ARG;
+    }
+    if (!(gamma > 1.0) || !(dx > 0) || (dim >= 2 && !(dy > 0)) || (dim == 3 && !(dz > 0))) {
+        set_error("need gamma > 1 and positive cell sizes");
+        return MLAU_ERR_ARG;
+    }
+    mlau_sim *s = new mlau_sim();
+    s->g = Geometry{dim, nx, ny, nz, xoff, yoff, zoff, (long long)nx * ny * nz, dx, dy, dz};
+    s->gamma = gamma;
+    s->odr = odr;
+    s->flux = flux;
+    s->nrk = nrk;
+    s->precision = precision;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        set_error("cudaStreamCreate: %s", cudaGetErrorString(e));
+        delete s;
+        return MLAU_ERR_CUDA;
+    }
+    s->timer.stream = s->stream;
+    int rc;
+    if (precision == MLAU_FP32_SPLIT) rc = split3d_alloc(s);
+    else if (dim == 3) rc = plain3d_alloc(s);
+    else if (dim == 2) rc = plain2d_alloc(s);
+    else rc = plain1d_alloc(s);
+    if (rc == MLAU_OK && dalloc(s, &s->d_red, 4)) rc = MLAU_ERR_NOMEM;
+    if (rc != MLAU_OK) {
+        mlau_sim_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return MLAU_OK;
+}
+
+int mlau_sim_destroy(mlau_sim *s)
+{
+    if (!s) return MLAU_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->timer.recs.clear();
+    if (s->sp) split3d_free(s);
+    for (void *p : s->allocs) cudaFree(p);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return MLAU_OK;
+}
+
+static int nvars(const Sim *s) { return 8; }
+
+int mlau_sim_upload(mlau_sim *s, const double *const *h)
+{
+    if (!s || !h) { set_error("null argument"); return MLAU_ERR_ARG; }
+    for (int v = 0; v < nvars(s); v++) {
+        if (s->g.dim == 1 && v == 5) continue;
+        MLAU_CUDA(cudaMemcpyAsync(s->f.s[v], h[v], sizeof(double) * s->g.n,
+                                  cudaMemcpyHostToDevice, s->stream));
+    }
+    return MLAU_OK;
+}
+
+int mlau_sim_download(mlau_sim *s, double *const *h)
+{
+    if (!s || !h) { set_error("null argument"); return MLAU_ERR_ARG; }
+    for (int v = 0; v < nvars(s); v++) {
+        if (s->g.dim == 1 && v == 5) continue;
+        MLAU_CUDA(cudaMemcpyAsync(h[v], s->f.s[v], sizeof(double) * s->g.n,
+                                  cudaMemcpyDeviceToHost, s->stream));
+    }
+    MLAU_CUDA(cudaStreamSynchronize(s->stream));
+    return MLAU_OK;
+}
+
+int mlau_sim_set_bx_1d(mlau_sim *s, double bx)
+{
+    if (!s || s->g.dim != 1) { set_error("not a 1D simulation"); return MLAU_ERR_ARG; }
+    s->bx1d = bx;
+    return MLAU_OK;
+}
+
+int mlau_sim_set_bc_1d(mlau_sim *s, int bc)
+{
+    if (!s || s->g.dim != 1 || (bc != MLAU_BC1D_OPEN && bc != MLAU_BC1D_PERIODIC)) {
+        set_error("bad 1D boundary request");
+        return MLAU_ERR_ARG;
+    }
+    s->bc1d = bc;
+    return MLAU_OK;
+}
+
+int mlau_sim_step(mlau_sim *s, double dt, int nsteps)
+{
+    if (!s || nsteps < 0 || !(dt == dt)) { set_error("bad step arguments"); return MLAU_ERR_ARG; }
+    for (int n = 0; n < nsteps; n++) {
+        int rc;
+        if (s->precision == MLAU_FP32_SPLIT) rc = split3d_step(s, dt);
+        else if (s->g.dim == 3) rc = plain3d_step(s, dt);
+        else if (s->g.dim == 2) rc = plain2d_step(s, dt);
+        else rc = plain1d_step(s, dt);
+        if (rc != MLAU_OK) return rc;
+    }
+    return MLAU_OK;
+}
+
+int mlau_sim_cfl(mlau_sim *s, double cfl, double dr, double vfast, double dt_old, double *dt_out,
+                 double *vmax_out)
+{
+    if (!s) { set_error("null simulation"); return MLAU_ERR_ARG; }
+    double cellmax = 0.0;
+    int rc = cfl_compute(s, &cellmax);
+    if (rc != MLAU_OK) return rc;
+    // vmax starts at vfast and takes a cell only when it is larger
+    // (cflcheck.hpp:5,24); NaN cells were excluded on the device.
+    const double vmax = (cellmax > vfast) ? cellmax : vfast;
+    if (vmax_out) *vmax_out = vmax;
+    double dt = dt_old;
+    if (std::isfinite(vmax)) dt = cfl * dr / vmax;
+    if (dt_out) *dt_out = dt;
+    return MLAU_OK;
+}
+
+int mlau_sim_sync(mlau_sim *s)
+{
+    if (!s) { set_error("null simulation"); return MLAU_ERR_ARG; }
+    MLAU_CUDA(cudaStreamSynchronize(s->stream));
+    return MLAU_OK;
+}
+
+void *mlau_sim_stream(mlau_sim *s) { return s ? (void *)s->stream : nullptr; }
+
+int mlau_sim_device_ptr(mlau_sim *s, int v, double **p)
+{
+    if (!s || !p || v < 0 || v >= 8) { set_error("bad variable index"); return MLAU_ERR_ARG; }
+    *p = s->f.s[v];
+    return MLAU_OK;
+}
+
+int mlau_sim_set_timing(mlau_sim *s, int on)
+{
+    if (!s) { set_error("null simulation"); return MLAU_ERR_ARG; }
+    int rc = s->timer.flush();
+    s->timer.on = (on != 0);
+    s->timer.reset();
+    return rc;
+}
+
+int mlau_sim_timing(mlau_sim *s, int kind, long *count, double *total_ms)
+{
+    if (!s || kind < 0 || kind >= KK_COUNT) { set_error("bad timing request"); return MLAU_ERR_ARG; }
+    int rc = s->timer.flush();
+    if (count) *count = s->timer.count[kind];
+    if (total_ms) *total_ms = s->timer.total_ms[kind];
+    return rc;
+}
+
+long long mlau_sim_device_bytes(mlau_sim *s) { return s ? s->bytes : 0; }
+
+int mlau_sim_launches_per_step(mlau_sim *s) { return s ? launches_per_step(s) : 0; }
+
+int mlau_sim_time_steps(mlau_sim *s, double dt, int nsteps, double *ms)
+{
+    if (!s || !ms) { set_error("null argument"); return MLAU_ERR_ARG; }
+    cudaEvent_t a, b;
+    MLAU_CUDA(cudaEventCreate(&a));
+    MLAU_CUDA(cudaEventCreate(&b));
+    MLAU_CUDA(cudaEventRecord(a, s->stream));
+    int rc = mlau_sim_step(s, dt, nsteps);
+    MLAU_CUDA(cudaEventRecord(b, s->stream));
+    MLAU_CUDA(cudaEventSynchronize(b));
+    float t = 0.f;
+    MLAU_CUDA(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = t;
+    return rc;
+}
+
+int mlau_pin_host(void *p, long long bytes)
+{
+    if (!p || bytes <= 0) { set_error("bad host range"); return MLAU_ERR_ARG; }
+    MLAU_CUDA(cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault));
+    return MLAU_OK;
+}
+
+int mlau_set_device(int dev)
+{
+    MLAU_CUDA(cudaSetDevice(dev));
+    return MLAU_OK;
+}
+
+int mlau_unpin_host(void *p)
+{
+    MLAU_CUDA(cudaHostUnregister(p));
+    return MLAU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Drop-in drivers with the reference's names.  One cached device context per
+// dimensionality; it is rebuilt when the geometry or scheme changes.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Scheme { int odr, flux, nrk; };
+std::mutex g_mu;
+bool g_scheme_init = false;
+Scheme g_scheme[4];
+int g_bc1d = MLAU_BC1D_OPEN;
+mlau_sim *g_ctx[4] = {nullptr, nullptr, nullptr, nullptr};
+
+int flux_from_name(const char *n)
+{
+    if (!n) return -1;
+    if (!strcmp(n, "mlau")) return MLAU_FLUX_MLAU;
+    if (!strcmp(n, "lhlld") || !strcmp(n, "hl3d2")) return MLAU_FLUX_LHLLD;
+    if (!strcmp(n, "hlld")) return MLAU_FLUX_HLLD;
+    if (!strcmp(n, "roe")) return MLAU_FLUX_ROE;
+    return -1;
+}
+
+void init_scheme()
+{
+    if (g_scheme_init) return;
+    g_scheme[3] = {2, MLAU_FLUX_LHLLD, 3};
+    g_scheme[2] = {2, MLAU_FLUX_LHLLD, 3};
+    g_scheme[1] = {1, MLAU_FLUX_LHLLD, 2};
+    const char *o = getenv("MLAU_ODR"), *r = getenv("MLAU_RK"), *f = getenv("MLAU_FLUX");
+    for (int d = 1; d <= 3; d++) {
+        if (o) g_scheme[d].odr = atoi(o);
+        if (r) g_scheme[d].nrk = atoi(r);
+        if (f && flux_from_name(f) >= 0) g_scheme[d].flux = flux_from_name(f);
+    }
+    g_scheme_init = true;
+}
+
+// Boundary tables of the problem program (3D/MPI/OTvortex/global.hpp:22-29).
+// Weak: a problem that defines them is checked; otherwise periodic is assumed.
+extern "C" {
+__attribute__((weak)) extern int dnxs[8];
+__attribute__((weak)) extern int dnys[8];
+__attribute__((weak)) extern int dnzs[8];
+}
+
+bool tables_periodic(int dim)
+{
+    int *t[3] = {dnxs, dnys, dnzs};
+    for (int d = 0; d < dim && d < 3; d++) {
+        if (!t[d]) continue;
+        for (int v = 0; v < 8; v++)
+            if (t[d][v] != 0) return false;
+    }
+    return true;
+}
+
+mlau_sim *get_ctx(int dim, int nx, int ny, int nz, int ox, int oy, int oz, double dx, double dy,
+                  double dz, double gamma)
+{
+    init_scheme();
+    const Scheme &sc = g_scheme[dim];
+    mlau_sim *c = g_ctx[dim];
+    if (c && c->g.nx == nx && c->g.ny == ny && c->g.nz == nz && c->g.ox == ox &&
+        c->g.oy == oy && c->g.oz == oz && c->odr == sc.odr && c->flux == sc.flux &&
+        c->nrk == sc.nrk) {
+        c->g.dx = dx;
+        c->g.dy = dy;
+        c->g.dz = dz;
+        c->gamma = gamma;
+        return c;
+    }
+    if (c) { mlau_sim_destroy(c); g_ctx[dim] = nullptr; }
+    if (mlau_sim_create(&c, dim, nx, ny, nz, ox, oy, oz, dx, dy, dz, gamma, sc.odr, sc.flux,
+                        sc.nrk, MLAU_FP64) != MLAU_OK)
+        return nullptr;
+    g_ctx[dim] = c;
+    return c;
+}
+
+void report(const char *who)
+{
+    fprintf(stderr, "%s: %s (arrays left unchanged)\n", who, mlau_last_error());
+}
+
+int run_dropin(mlau_sim *c, double *const *h, double dt)
+{
+    int rc = mlau_sim_upload(c, (const double *const *)h);
+    if (rc == MLAU_OK) rc = mlau_sim_step(c, dt, 1);
+    if (rc == MLAU_OK) rc = mlau_sim_download(c, h);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mlau_set_scheme(int dim, int odr, int flux, int nrk)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    init_scheme();
+    if (dim < 1 || dim > 3 || odr < 1 || odr > 4 || flux < 0 || flux > 3 || nrk < 1 || nrk > 3) {
+        set_error("mlau_set_scheme: out of range");
+        return MLAU_ERR_ARG;
+    }
+    g_scheme[dim] = {odr, flux, nrk};
+    return MLAU_OK;
+}
+
+int mlau_set_bc_1d(int bc)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (bc != MLAU_BC1D_OPEN && bc != MLAU_BC1D_PERIODIC) {
+        set_error("mlau_set_bc_1d: bad boundary");
+        return MLAU_ERR_ARG;
+    }
+    g_bc1d = bc;
+    return MLAU_OK;
+}
+
+void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                  double *by, double *bz, double dt, double dx, double dy, double dz, int nx,
+                  int ny, int nz, int xoff, int yoff, int zoff, double gamma, int mpi_rank,
+                  int mpi_numx, int mpi_numy, int mpi_numz)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mpi_rank != 0 || mpi_numx != 1 || mpi_numy != 1 || mpi_numz != 1) {
+        set_error("single-GPU build: mpi_rank=0 and mpi_num{x,y,z}=1 required");
+        report("mhd_fd_ct_3d");
+        return;
+    }
+    if (!tables_periodic(3)) {
+        set_error("only periodic boundaries (dnxs/dnys/dnzs all 0) are implemented");
+        report("mhd_fd_ct_3d");
+        return;
+    }
+    mlau_sim *c = get_ctx(3, nx, ny, nz, xoff, yoff, zoff, dx, dy, dz, gamma);
+    double *h[8] = {ro, mx, my, mz, en, bx, by, bz};
+    if (!c || run_dropin(c, h, dt) != MLAU_OK) report("mhd_fd_ct_3d");
+}
+
+void mhd_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                  double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                  int xoff, int yoff, double gamma)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!tables_periodic(2)) {
+        set_error("only periodic boundaries (dnxs/dnys all 0) are implemented");
+        report("mhd_fd_ct_2d");
+        return;
+    }
+    mlau_sim *c = get_ctx(2, nx, ny, 1, xoff, yoff, 0, dx, dy, 1.0, gamma);
+    double *h[8] = {ro, mx, my, mz, en, bx, by, bz};
+    if (!c || run_dropin(c, h, dt) != MLAU_OK) report("mhd_fd_ct_2d");
+}
+
+void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                      double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                      int xoff, int yoff, double gamma, int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    if (mpi_rank != 0 || mpi_numx != 1 || mpi_numy != 1) {
+        set_error("single-GPU build: mpi_rank=0 and mpi_num{x,y}=1 required");
+        report("mhd_fd_ct_2d");
+        return;
+    }
+    mhd_fd_ct_2d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma);
+}
+
+void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,
+                 double *bz, double bx, double dt, double dx, int nx, int xoff, double gamma)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    mlau_sim *c = get_ctx(1, nx, 1, 1, xoff, 0, 0, dx, 1.0, 1.0, gamma);
+    if (!c) { report("mhd_fd4c_1d"); return; }
+    c->bx1d = bx;
+    c->bc1d = g_bc1d;
+    double *h[8] = {ro, mx, my, mz, en, nullptr, by, bz};
+    if (run_dropin(c, h, dt) != MLAU_OK) report("mhd_fd4c_1d");
+}
+
+}  // extern "C"

@@ -1,0 +1,62 @@
+// Internal simulation object behind the mlau_sim handle.
+#pragma once
+
+#include "common.cuh"
+
+namespace mlau {
+
+// Device fields of the plain FP64 step, one padded array each.
+struct PlainFields {
+    double *s[8];        // state ro, mx, my, mz, en, bx, by, bz
+    double *u0[8];       // copy of the state at the start of the step (U^n)
+    double *vx, *vy, *vz, *pr, *m2, *cx, *cy, *cz;
+    double *dv[3];       // shock sensors dvx, dvy, dvz
+    double *ct[3];       // CT Alfven-upwind weights at x-y (ct0), y-z (ct1), z-x (ct2) edges
+    double *ul[7], *ur[7];     // face states (ro, vn, vt, vu, bt, bu, pr)
+    double *ql[2], *qr[2];     // linear central parts of the two tangential B fluxes
+    double *F[3][7];     // face fluxes per direction: (ro, mn, mt, mu, bt, bu, en)
+    double *FC[3][2];    // central parts of the bt and bu fluxes
+    double *e[3];        // edge EMFs ex, ey, ez
+};
+
+struct Geometry {
+    int dim;
+    int nx, ny, nz, ox, oy, oz;
+    long long n;  // nx*ny*nz
+    double dx, dy, dz;
+};
+
+struct SplitFields;  // FP32-split workspace (split3d.cu)
+
+struct Sim {
+    Geometry g;
+    double gamma;
+    int odr, flux, nrk, precision;
+    int bc1d = MLAU_BC1D_OPEN;
+    double bx1d = 0.0;
+    cudaStream_t stream = nullptr;
+    PlainFields f{};
+    SplitFields *sp = nullptr;
+    std::vector<void *> allocs;
+    long long bytes = 0;
+    double *d_red = nullptr;   // device scratch for reductions (2 doubles)
+    int *d_flag = nullptr;     // device status flag
+    KernelTimer timer;
+};
+
+int plain3d_alloc(Sim *s);
+int plain3d_step(Sim *s, double dt);
+int plain2d_alloc(Sim *s);
+int plain2d_step(Sim *s, double dt);
+int plain1d_alloc(Sim *s);
+int plain1d_step(Sim *s, double dt);
+int split3d_alloc(Sim *s);
+int split3d_step(Sim *s, double dt);
+void split3d_free(Sim *s);
+int cfl_compute(Sim *s, double *vmax_out);
+int launches_per_step(const Sim *s);
+
+// Allocate one padded array per call; recorded for release at destroy.
+int dalloc(Sim *s, double **p, long long count);
+
+}  // namespace mlau

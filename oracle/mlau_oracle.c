@@ -15,6 +15,13 @@
 #include "mlau_oracle.h"
 #include "oracle_point.h"
 
+/* Phase hook of the op-counting build (oracle/opcount.cpp); no-op here.
+ * 0 cell B + primitives, 1 CT weights + shock sensors, 2 reconstruction,
+ * 3 Riemann flux, 4 edge EMF, 5 RK update + CT curl. */
+#ifndef ORACLE_PHASE
+#define ORACLE_PHASE(p) ((void)0)
+#endif
+
 #define IDX3(i, j, k) ((long)nx * ((long)ny * (k) + (j)) + (i))
 
 static double *alloc_d(long n)
@@ -98,6 +105,7 @@ static void sweep_pencil(const sweep_in *S, long base, long st, int len, int odr
                          double *ul, double *ur, double *qlt, double *qrt, double *qlu,
                          double *qru)
 {
+    ORACLE_PHASE(2);
     for (int i = 2; i < len - 2; i++) {
         long c = base + st * i;
         double q[7][5];
@@ -144,6 +152,7 @@ static void sweep_pencil(const sweep_in *S, long base, long st, int len, int odr
             qru[i] = ra - br * rb;
         }
     }
+    ORACLE_PHASE(3);
     for (int i = 3; i < len - 2; i++) {
         long c = base + st * i;
         double bn = 0.5 * (S->bface[c] + S->bface[c]);
@@ -165,31 +174,33 @@ static void sweep_pencil(const sweep_in *S, long base, long st, int len, int odr
     }
 }
 
-/* Corner (edge) EMF contribution along an axis with stride st: for edge index
- * j in [3, len-2) of a pencil, ``e += sgn*0.5*((ul0+ur0) + w*(ul1+ur1))`` with
- * ul/ur the linear face interpolations of the upwind (fu) and central (fc)
- * parts, w = ct or 1-ct (mhd_fd_ct_3d.c:494-585 and siblings). */
+/* Corner (edge) EMF contribution along an axis with stride st (one pencil):
+ * the linear face interpolations of the upwind (fu) and central (fc) parts are
+ * formed once per window j in [2, len-2), then for edges j in [3, len-2)
+ * ``e += (+-0.5)*((ul0+ur0) + w*(ul1+ur1))`` with w = ct or 1-ct
+ * (mhd_fd_ct_3d.c:494-585 and siblings). */
 static void emf_pencil(const double *fu, const double *fc, const double *ctw, int one_minus,
                        double sgn, double *e, long base, long st, int len, int odr)
 {
-    for (int j = 3; j < len - 2; j++) {
+    double *buf = alloc_d(4L * (len + 1));
+    double *ul0 = buf, *ur0 = buf + (len + 1), *ul1 = buf + 2 * (len + 1), *ur1 = buf + 3 * (len + 1);
+    for (int j = 2; j < len - 2; j++) {
         long c = base + st * j;
-        double a[5], b[5], ul0, ur0, ul1, ur1, dummy;
-        for (int m = 0; m < 5; m++) {
-            a[m] = fu[c + st * (m - 3)];
-            b[m] = fc[c + st * (m - 3)];
-        }
-        o_lin_lr(odr, a, &ul0, &dummy);
-        o_lin_lr(odr, b, &ul1, &dummy);
+        double a[5], b[5];
         for (int m = 0; m < 5; m++) {
             a[m] = fu[c + st * (m - 2)];
             b[m] = fc[c + st * (m - 2)];
         }
-        o_lin_lr(odr, a, &dummy, &ur0);
-        o_lin_lr(odr, b, &dummy, &ur1);
-        double w = one_minus ? (1.0 - ctw[c]) : ctw[c];
-        e[c] += sgn * 0.5 * ((ul0 + ur0) + w * (ul1 + ur1));
+        o_lin_lr(odr, a, &ul0[j + 1], &ur0[j]);
+        o_lin_lr(odr, b, &ul1[j + 1], &ur1[j]);
     }
+    const double h = (sgn > 0) ? 0.5 : -0.5;
+    for (int j = 3; j < len - 2; j++) {
+        long c = base + st * j;
+        double w = one_minus ? (1.0 - ctw[c]) : ctw[c];
+        e[c] += h * ((ul0[j] + ur0[j]) + w * (ul1[j] + ur1[j]));
+    }
+    free(buf);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -223,6 +234,7 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
         double ra, rb;
         rk_coef(nrk, rk, &ra, &rb);
 
+        ORACLE_PHASE(0);
         /* cell-centred B (:186-220) and its periodic fill (:221-238) */
 #pragma omp parallel for
         for (int k = 0; k < nz; k++) {
@@ -263,6 +275,7 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
             ct0[s] = ct1[s] = ct2[s] = 0.5;
         }
 
+        ORACLE_PHASE(1);
         /* Alfven-upwind CT weights (:264-340) */
         const double eps = 1e-6;
 #pragma omp parallel for
@@ -355,6 +368,7 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
             }
         }
 
+        ORACLE_PHASE(4);
         /* edge EMFs (:494-585, :702-793, :910-1001).  F[d][4] is the flux of
          * the first tangential B (t), F[d][5] of the second (u):
          *   X: t=y, u=z;  Y: t=z, u=x;  Z: t=x, u=y. */
@@ -383,6 +397,7 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
             for (int i = 0; i < nx; i++)
                 emf_pencil(F[2][5], FC[2][1], ct1, 0, +1.0, ex, IDX3(i, 0, k), sy, ny, odr);
 
+        ORACLE_PHASE(5);
         /* cell-centred update (:1003-1078).  Flux component per direction
          * for (ro, mx, my, mz, en): X (0,1,2,3,6), Y (0,3,1,2,6), Z (0,2,3,1,6). */
         static const int cmp[3][5] = {{0, 1, 2, 3, 6}, {0, 3, 1, 2, 6}, {0, 2, 3, 1, 6}};
@@ -466,6 +481,7 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
     for (int rk = 0; rk < nrk; rk++) {
         double ra, rb;
         rk_coef(nrk, rk, &ra, &rb);
+        ORACLE_PHASE(0);
         /* cell-centred B (:172-201) */
 #pragma omp parallel for
         for (int j = 0; j < ny; j++)
@@ -495,6 +511,7 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
             ez[s] = 0.0;
             ctw[s] = 0.5;
         }
+        ORACLE_PHASE(1);
         /* CT weights (:224-249) */
         const double eps = 1e-6;
 #pragma omp parallel for
@@ -542,6 +559,7 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
             free(ur);
             free(q);
         }
+        ORACLE_PHASE(4);
         /* Ez from x-faces along Y (:364-402) and from y-faces along X (:495-533).
          * The 2D reference restricts the x-face part to rows j in [3,ny-2) via
          * its loops; emf_pencil covers the same edges. */
@@ -552,6 +570,7 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
         for (int j = 3; j < ny - 2; j++)
             emf_pencil(FY[5], fcy, ctw, 0, +1.0, ez, (long)nx * j, 1, nx, odr);
 
+        ORACLE_PHASE(5);
         /* cell-centred update incl. Bz (:535-592).  Components per direction
          * for (ro, mx, my, mz, bz, en): X (0,1,2,3,5,6), Y (0,3,1,2,4,6). */
         static const int cx2[6] = {0, 1, 2, 3, 5, 6}, cy2[6] = {0, 3, 1, 2, 4, 6};

@@ -1,0 +1,109 @@
+"""Generate the golden vectors in this directory from the reference itself.
+
+Run here, where the reference tree is present:
+    python tests/golden/make_golden.py
+It compiles the reference's own drivers (oracle/build.py, from the reference
+sources) for each scheme variant, runs them on seeded inputs, and stores the
+inputs and outputs.  3D/2D states are stored as their interior cells only: the
+inputs are periodic (ghosts = periodic images) and every output ghost is a
+periodic image too, so tests rebuild the ghosts with a periodic pad.  1D states
+(open boundaries) are stored whole.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from mlau_gb300 import ics  # noqa: E402
+from oracle import Ref  # noqa: E402
+
+OFF = 4
+CASES_3D = [  # (name, n, mach, odr, flux, seed)
+    ("3d_mlau_o4", 8, 0.9, 4, "mlau", 1),
+    ("3d_lhlld_o4", 8, 0.9, 4, "lhlld", 2),
+    ("3d_hlld_o4", 8, 0.9, 4, "hlld", 3),
+    ("3d_roe_o4", 8, 0.9, 4, "roe", 4),
+    ("3d_mlau_o2", 8, 0.9, 2, "mlau", 5),
+    ("3d_lhlld_o3", 8, 0.9, 3, "lhlld", 6),
+    ("3d_mlau_o4_lowmach", 8, 1e-2, 4, "mlau", 7),
+]
+CASES_2D = [
+    ("2d_lhlld_o4", 16, 4, "lhlld", 1),
+    ("2d_mlau_o4", 16, 4, "mlau", 2),
+    ("2d_hlld_o2", 16, 2, "hlld", 3),
+    ("2d_roe_o4", 16, 4, "roe", 4),
+    ("2d_lhlld_o1", 16, 1, "lhlld", 5),
+]
+CASES_1D = [  # (name, n, odr, flux, bc, seed)
+    ("1d_mlau_o2_open", 64, 2, "mlau", "open", 1),
+    ("1d_lhlld_o1_open", 64, 1, "lhlld", "open", 2),
+    ("1d_hlld_o4_open", 64, 4, "hlld", "open", 3),
+    ("1d_roe_o3_open", 64, 3, "roe", "open", 4),
+    ("1d_mlau_o4_periodic", 64, 4, "mlau", "periodic", 5),
+]
+STEPS = (1, 4)
+
+
+def interior(a, dim):
+    return np.ascontiguousarray(a[(slice(OFF, -OFF),) * dim])
+
+
+def main():
+    for name, n, mach, odr, flux, seed in CASES_3D:
+        st, m = ics.turbulence_3d(n=n, mach=mach, seed=seed, odr=odr)
+        dt = 0.3 * m["dx"] / m["vfast"]
+        out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "odr": odr, "flux": flux}
+        for k, v in st.items():
+            out["in_" + k] = interior(v, 3)
+        s = ics.copy_state(st)
+        done = 0
+        for nstep in STEPS:
+            for _ in range(nstep - done):
+                Ref.step3d(s, dt, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux)
+            done = nstep
+            for k, v in s.items():
+                out[f"out{nstep}_" + k] = interior(v, 3)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, n, odr, flux, seed in CASES_2D:
+        st, m = ics.turbulence_2d(n=n, seed=seed, odr=odr, vrms=1.2)
+        dt = 0.3 * m["dx"] / m["vfast"]
+        out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "odr": odr, "flux": flux}
+        for k, v in st.items():
+            out["in_" + k] = interior(v, 2)
+        s = ics.copy_state(st)
+        done = 0
+        for nstep in STEPS:
+            for _ in range(nstep - done):
+                Ref.step2d(s, dt, m["dx"], m["dy"], odr=odr, flux=flux)
+            done = nstep
+            for k, v in s.items():
+                out[f"out{nstep}_" + k] = interior(v, 2)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, n, odr, flux, bc, seed in CASES_1D:
+        st, m = ics.riemann_1d(n=n, seed=seed)
+        from oracle import Port
+        dt = Port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
+        out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "bx": m["bx"], "odr": odr,
+               "flux": flux, "bc": bc}
+        for k, v in st.items():
+            out["in_" + k] = v.copy()
+        s = ics.copy_state(st)
+        done = 0
+        for nstep in STEPS:
+            for _ in range(nstep - done):
+                Ref.step1d(s, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux, bc=bc)
+            done = nstep
+            for k, v in s.items():
+                out[f"out{nstep}_" + k] = v.copy()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", len(CASES_3D) + len(CASES_2D) + len(CASES_1D), "golden cases to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,78 @@
+"""CPU tests of the C ABI library: it loads, exports every symbol that
+include/*.h declares (with C and, for the drop-in drivers, the reference's C++
+linkage), and rejects bad arguments before touching the GPU."""
+import ctypes as C
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(", text, flags=re.M):
+            if m.group(1) not in ("if", "return", "sizeof"):
+                names.append(m.group(1))
+    return sorted(set(names))
+
+
+def exported():
+    import mlau_gb300 as M
+    out = subprocess.run(["nm", "-D", "--defined-only", M.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if line.strip()}
+
+
+def test_library_loads(gpu_lib):
+    assert os.path.exists(gpu_lib.LIB_PATH)
+
+
+def test_header_symbols_exported(gpu_lib):
+    syms = exported()
+    missing = [n for n in header_functions() if n not in syms]
+    assert not missing, missing
+    assert len(header_functions()) >= 20
+
+
+def test_cxx_linkage_drivers_exported(gpu_lib):
+    syms = exported()
+    for mangled in ("_Z12mhd_fd_ct_3dPdS_S_S_S_S_S_S_ddddiiiiiidiiii",
+                    "_Z12mhd_fd_ct_2dPdS_S_S_S_S_S_S_dddiiiid",
+                    "_Z12mhd_fd_ct_2dPdS_S_S_S_S_S_S_dddiiiidiii",
+                    "_Z11mhd_fd4c_1dPdS_S_S_S_S_S_dddiid"):
+        assert mangled in syms
+
+
+def test_create_rejects_bad_geometry(gpu_lib):
+    L = gpu_lib.lib()
+    h = C.c_void_p()
+    # interior narrower than the ghost depth
+    rc = L.mlau_sim_create(C.byref(h), 3, 10, 10, 10, 4, 4, 4, 1.0, 1.0, 1.0, 5 / 3, 4, 0, 3, 0)
+    assert rc == -1 and "interior" in gpu_lib.last_error()
+    rc = L.mlau_sim_create(C.byref(h), 3, 16, 16, 16, 4, 4, 4, 1.0, 1.0, 1.0, 5 / 3, 7, 0, 3, 0)
+    assert rc == -1
+    rc = L.mlau_sim_create(C.byref(h), 2, 16, 16, 1, 4, 4, 0, 1.0, 1.0, 1.0, 0.9, 4, 0, 3, 0)
+    assert rc == -1 and "gamma" in gpu_lib.last_error()
+    rc = L.mlau_sim_create(C.byref(h), 1, 64, 1, 1, 4, 0, 0, 1.0, 1.0, 1.0, 2.0, 2, 0, 3, 1)
+    assert rc == -1 and "precision" in gpu_lib.last_error()
+
+
+def test_set_scheme_validation(gpu_lib):
+    L = gpu_lib.lib()
+    assert L.mlau_set_scheme(3, 5, 0, 3) == -1
+    assert L.mlau_set_scheme(3, 4, 9, 3) == -1
+    assert L.mlau_set_bc_1d(7) == -1
+
+
+def test_loading_fails_loudly_without_library(tmp_path, monkeypatch):
+    import mlau_gb300 as M
+    monkeypatch.setattr(M, "_lib", None)
+    monkeypatch.setattr(M, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(M.MlauError):
+        M.lib()

@@ -1,0 +1,147 @@
+"""CPU tests of the oracle: pinned to the reference and to its golden vectors,
+plus the invariants the reference's scheme guarantees."""
+import itertools
+
+import numpy as np
+import pytest
+
+from _util import equal_values, golden_cases, load_golden
+from mlau_gb300 import ics
+from oracle import Ref
+
+
+@pytest.mark.parametrize("name", golden_cases("3d"))
+def test_port_matches_golden_3d(port, name):
+    prm, s, outs = load_golden(name)
+    done = 0
+    for n in sorted(outs):
+        for _ in range(n - done):
+            port.step3d(s, prm["dt"], prm["dx"], prm["dx"], prm["dx"], gamma=prm["gamma"],
+                        odr=prm["odr"], flux=prm["flux"])
+        done = n
+        assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
+
+
+@pytest.mark.parametrize("name", golden_cases("2d"))
+def test_port_matches_golden_2d(port, name):
+    prm, s, outs = load_golden(name)
+    done = 0
+    for n in sorted(outs):
+        for _ in range(n - done):
+            port.step2d(s, prm["dt"], prm["dx"], prm["dx"], gamma=prm["gamma"], odr=prm["odr"],
+                        flux=prm["flux"])
+        done = n
+        assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
+
+
+@pytest.mark.parametrize("name", golden_cases("1d"))
+def test_port_matches_golden_1d(port, name):
+    prm, s, outs = load_golden(name)
+    done = 0
+    for n in sorted(outs):
+        for _ in range(n - done):
+            port.step1d(s, prm["bx"], prm["dt"], prm["dx"], gamma=prm["gamma"], odr=prm["odr"],
+                        flux=prm["flux"], bc=prm["bc"])
+        done = n
+        assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
+
+
+needs_ref = pytest.mark.skipif(not Ref.available(), reason="reference tree not present")
+
+
+@needs_ref
+@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe"))))
+def test_port_matches_reference_3d(port, odr, flux):
+    st, m = ics.turbulence_3d(n=6, ny=7, nz=5, mach=0.8, seed=odr * 7 + len(flux), odr=odr)
+    # inconsistent ghosts: the step must read exactly the reference's cells
+    rng = np.random.default_rng(1)
+    for k in st:
+        g = st[k].copy()
+        g[:4] *= 1 + 1e-3 * rng.random(g[:4].shape)
+        st[k] = np.ascontiguousarray(g)
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    for _ in range(2):
+        port.step3d(a, 1e-3, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux)
+        Ref.step3d(b, 1e-3, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux)
+    assert equal_values(a, b)
+
+
+@needs_ref
+@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe"))))
+def test_port_matches_reference_2d(port, odr, flux):
+    st, m = ics.turbulence_2d(n=20, ny=14, seed=odr + 3, odr=odr, vrms=1.3)
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    for _ in range(3):
+        port.step2d(a, 2e-3, m["dx"], m["dy"], odr=odr, flux=flux)
+        Ref.step2d(b, 2e-3, m["dx"], m["dy"], odr=odr, flux=flux)
+    assert equal_values(a, b)
+
+
+@needs_ref
+@pytest.mark.parametrize("bc", ("open", "periodic"))
+@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe"))))
+def test_port_matches_reference_1d(port, odr, flux, bc):
+    st, m = ics.riemann_1d(n=48, seed=odr * 5 + len(flux))
+    dt = port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    for _ in range(6):
+        port.step1d(a, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux, bc=bc)
+        Ref.step1d(b, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux, bc=bc)
+    assert equal_values(a, b)
+
+
+@needs_ref
+@pytest.mark.parametrize("nrk", (1, 2))
+def test_port_matches_reference_rk_order(port, nrk):
+    st, m = ics.turbulence_3d(n=6, mach=0.5, seed=9)
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    port.step3d(a, 1e-3, m["dx"], m["dy"], m["dz"], nrk=nrk)
+    Ref.step3d(b, 1e-3, m["dx"], m["dy"], m["dz"], nrk=nrk)
+    assert equal_values(a, b)
+
+
+def test_port_div_b_preserved(port):
+    """CT keeps the scheme's discrete div B at round-off (mhd_fd_ct_3d.c:80-88)."""
+    st, m = ics.turbulence_3d(n=10, mach=0.3, seed=2)
+    d0 = ics.div_b_3d(st, m["dx"], m["dy"], m["dz"])
+    for _ in range(10):
+        port.step3d(st, 2e-3, m["dx"], m["dy"], m["dz"])
+    d1 = ics.div_b_3d(st, m["dx"], m["dy"], m["dz"])
+    assert d0 < 1e-13 and d1 < 1e-12
+
+
+def test_port_zero_guard_2d(port):
+    """Identically zero vz and Bz stay exactly zero (mhd_eigen.h:516-529)."""
+    st, m = ics.turbulence_2d(n=16, seed=4)
+    assert not st["mz"].any() and not st["bz"].any()
+    for _ in range(5):
+        port.step2d(st, 2e-3, m["dx"], m["dy"])
+    assert not st["mz"].any() and not st["bz"].any()
+
+
+def test_port_thread_count_independent(port):
+    """The step has no reductions: results do not depend on thread count."""
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import sys,numpy as np; sys.path.insert(0,%r); from oracle import Port; "
+        "from mlau_gb300 import ics; st,m=ics.turbulence_3d(n=8,mach=0.5,seed=3); "
+        "Port.step3d(st,1e-3,m['dx'],m['dy'],m['dz']); np.save(sys.argv[1], st['en'])"
+    ) % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for t in ("1", "4"):
+        path = f"/tmp/mlau_thr_{os.getpid()}_{t}.npy"
+        subprocess.run([sys.executable, "-c", code, path], check=True,
+                       env={**os.environ, "OMP_NUM_THREADS": t})
+        outs.append(np.load(path))
+        os.remove(path)
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_cfl_oracle_matches_formula(port):
+    st, m = ics.turbulence_3d(n=8, mach=0.3, seed=5)
+    dt, vmax = port.cfl3d(st, 0.4, m["dx"], 0.0, 1.0)
+    assert vmax > 0 and abs(dt - 0.4 * m["dx"] / vmax) < 1e-18
+    dt2, vm2 = port.cfl3d(st, 0.4, m["dx"], 1e9, 1.0)
+    assert vm2 == 1e9
