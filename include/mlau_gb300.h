@@ -89,6 +89,12 @@ void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, dou
  * the defaults at first use. */
 int mlau_set_scheme(int dim, int odr, int flux, int nrk);
 int mlau_set_bc_1d(int bc);
+/* Arithmetic of the drop-in 3D driver: MLAU_FP64 (default; the reference's
+ * arithmetic bit for bit) or MLAU_FP32_SPLIT. */
+int mlau_set_precision(int dim, int precision);
+/* Free the device memory cached by the drop-in drivers (it is kept between
+ * calls so that a time loop does not reallocate every step). */
+void mlau_release_dropin(void);
 const char *mlau_last_error(void);
 void mlau_clear_error(void);
 

@@ -65,6 +65,8 @@ def _bind(lib):
     lib.mlau_set_device.argtypes = [i]
     lib.mlau_set_scheme.argtypes = [i, i, i, i]
     lib.mlau_set_bc_1d.argtypes = [i]
+    lib.mlau_set_precision.argtypes = [i, i]
+    lib.mlau_release_dropin.restype = None
     lib.mhd_fd_ct_3d.argtypes = [pd] * 8 + [d] * 4 + [i] * 6 + [d] + [i] * 4
     lib.mhd_fd_ct_3d.restype = None
     lib.mhd_fd_ct_2d.argtypes = [pd] * 8 + [d] * 3 + [i] * 4 + [d]
@@ -111,6 +113,14 @@ def set_scheme(dim: int, odr: int, flux="lhlld", nrk: int = 3):
 
 def set_bc_1d(bc: str):
     _check(lib().mlau_set_bc_1d(BC1D[bc]))
+
+
+def set_precision(dim: int, precision: int):
+    _check(lib().mlau_set_precision(dim, precision))
+
+
+def release_dropin():
+    lib().mlau_release_dropin()
 
 
 def mhd_fd_ct_3d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, dz, nx, ny, nz, xoff, yoff, zoff,

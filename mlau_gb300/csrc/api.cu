@@ -105,10 +105,11 @@ static int check_geometry(int dim, int nx, int ny, int nz, int ox, int oy, int o
 
 int launches_per_step(const Sim *s)
 {
-    if (s->precision == MLAU_FP32_SPLIT) return 1 + 3 * s->nrk + 0;  // refined in split3d
+    // kernels per RK stage (device-to-device copies are not counted)
+    if (s->precision == MLAU_FP32_SPLIT) return s->nrk * 7;
     if (s->g.dim == 3) return s->nrk * 10;
     if (s->g.dim == 2) return s->nrk * 8;
-    return s->nrk * 4;
+    return s->nrk * 4 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
 }
 
 }  // namespace mlau
@@ -340,7 +341,7 @@ int mlau_unpin_host(void *p)
 // ---------------------------------------------------------------------------
 namespace {
 
-struct Scheme { int odr, flux, nrk; };
+struct Scheme { int odr, flux, nrk, precision; };
 std::mutex g_mu;
 bool g_scheme_init = false;
 Scheme g_scheme[4];
@@ -360,9 +361,9 @@ int flux_from_name(const char *n)
 void init_scheme()
 {
     if (g_scheme_init) return;
-    g_scheme[3] = {2, MLAU_FLUX_LHLLD, 3};
-    g_scheme[2] = {2, MLAU_FLUX_LHLLD, 3};
-    g_scheme[1] = {1, MLAU_FLUX_LHLLD, 2};
+    g_scheme[3] = {2, MLAU_FLUX_LHLLD, 3, MLAU_FP64};
+    g_scheme[2] = {2, MLAU_FLUX_LHLLD, 3, MLAU_FP64};
+    g_scheme[1] = {1, MLAU_FLUX_LHLLD, 2, MLAU_FP64};
     const char *o = getenv("MLAU_ODR"), *r = getenv("MLAU_RK"), *f = getenv("MLAU_FLUX");
     for (int d = 1; d <= 3; d++) {
         if (o) g_scheme[d].odr = atoi(o);
@@ -399,7 +400,7 @@ mlau_sim *get_ctx(int dim, int nx, int ny, int nz, int ox, int oy, int oz, doubl
     mlau_sim *c = g_ctx[dim];
     if (c && c->g.nx == nx && c->g.ny == ny && c->g.nz == nz && c->g.ox == ox &&
         c->g.oy == oy && c->g.oz == oz && c->odr == sc.odr && c->flux == sc.flux &&
-        c->nrk == sc.nrk) {
+        c->nrk == sc.nrk && c->precision == sc.precision) {
         c->g.dx = dx;
         c->g.dy = dy;
         c->g.dz = dz;
@@ -408,7 +409,7 @@ mlau_sim *get_ctx(int dim, int nx, int ny, int nz, int ox, int oy, int oz, doubl
     }
     if (c) { mlau_sim_destroy(c); g_ctx[dim] = nullptr; }
     if (mlau_sim_create(&c, dim, nx, ny, nz, ox, oy, oz, dx, dy, dz, gamma, sc.odr, sc.flux,
-                        sc.nrk, MLAU_FP64) != MLAU_OK)
+                        sc.nrk, sc.precision) != MLAU_OK)
         return nullptr;
     g_ctx[dim] = c;
     return c;
@@ -439,8 +440,31 @@ int mlau_set_scheme(int dim, int odr, int flux, int nrk)
         set_error("mlau_set_scheme: out of range");
         return MLAU_ERR_ARG;
     }
-    g_scheme[dim] = {odr, flux, nrk};
+    g_scheme[dim].odr = odr;
+    g_scheme[dim].flux = flux;
+    g_scheme[dim].nrk = nrk;
     return MLAU_OK;
+}
+
+int mlau_set_precision(int dim, int precision)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    init_scheme();
+    if (dim < 1 || dim > 3 || (precision != MLAU_FP64 && !(precision == MLAU_FP32_SPLIT && dim == 3))) {
+        set_error("mlau_set_precision: precision %d not available for dim %d", precision, dim);
+        return MLAU_ERR_ARG;
+    }
+    g_scheme[dim].precision = precision;
+    return MLAU_OK;
+}
+
+void mlau_release_dropin(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (int d = 1; d <= 3; d++) {
+        if (g_ctx[d]) mlau_sim_destroy(g_ctx[d]);
+        g_ctx[d] = nullptr;
+    }
 }
 
 int mlau_set_bc_1d(int bc)

@@ -177,10 +177,14 @@ MLAU_HD void zero_guard(const T q[7][5], T ul[7], T ur[7])
     }
 }
 
+// Alfven/entropy projection of the stencil q (variables x points) with the
+// eigenvectors of the centre state qc.  Linear in q: the FP32-split mode
+// passes perturbations from the cell centre here.
 template <class T>
-MLAU_HD void reconst_alfven(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+MLAU_HD void reconst_alfven_core(int odr, const T q[7][5], const T qc[7], T bn, T gamma, T ul[7],
+                                 T ur[7])
 {
-    const T ro = q[0][2], by = q[4][2], bz = q[5][2], pr = q[6][2];
+    const T ro = qc[0], by = qc[4], bz = qc[5], pr = qc[6];
     T iro = T(1.0) / ro;
     T cs2 = gamma * pr * iro;
     T ca2 = bn * bn * iro;
@@ -223,6 +227,13 @@ MLAU_HD void reconst_alfven(int odr, const T q[7][5], T bn, T gamma, T ul[7], T 
     ur[4] = T(0.5) * wr[3] - T(0.5) * wr[4];
     ur[5] = T(0.5) * wr[5] - T(0.5) * wr[6];
     ur[6] = wr[2] - byh * wr[3] + byh * wr[4] - bzh * wr[5] + bzh * wr[6];
+}
+
+template <class T>
+MLAU_HD void reconst_alfven(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+{
+    const T qc[7] = {q[0][2], q[1][2], q[2][2], q[3][2], q[4][2], q[5][2], q[6][2]};
+    reconst_alfven_core(odr, q, qc, bn, gamma, ul, ur);
     zero_guard(q, ul, ur);
 }
 
@@ -349,10 +360,11 @@ MLAU_HD void back_full(const Eigen7<T> &E, const T wl[7], T ul[7])
 }
 
 template <class T>
-MLAU_HD void reconst_full(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+MLAU_HD void reconst_full_core(int odr, const T q[7][5], const T qc[7], T bn, T gamma, T ul[7],
+                               T ur[7])
 {
     Eigen7<T> E;
-    eigen_full(q[0][2], q[1][2], bn, q[4][2], q[5][2], q[6][2], gamma, E);
+    eigen_full(qc[0], qc[1], bn, qc[4], qc[5], qc[6], gamma, E);
     T w[7][5];
 #pragma unroll
     for (int m = 0; m < 5; m++) {
@@ -366,6 +378,13 @@ MLAU_HD void reconst_full(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur
     for (int n = 0; n < 7; n++) rec_lr(odr, w[n], wl[n], wr[n]);
     back_full(E, wl, ul);
     back_full(E, wr, ur);
+}
+
+template <class T>
+MLAU_HD void reconst_full(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+{
+    const T qc[7] = {q[0][2], q[1][2], q[2][2], q[3][2], q[4][2], q[5][2], q[6][2]};
+    reconst_full_core(odr, q, qc, bn, gamma, ul, ur);
     zero_guard(q, ul, ur);
 }
 
@@ -376,9 +395,12 @@ MLAU_HD void reconst_full(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur
 // ---------------------------------------------------------------------------
 enum { FLUX_MLAU = 0, FLUX_LHLLD = 1, FLUX_HLLD = 2, FLUX_ROE = 3 };
 
-// calc_flux_mlau, mhd_flux.h:26-213
-template <class T>
-MLAU_HD void flux_mlau(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *f)
+// calc_flux_mlau, mhd_flux.h:26-213.  With JUMPS, the total-pressure jump
+// ptr-ptl (jp) and normal-velocity jump vnr-vnl (jv) come from the caller,
+// formed from split (base + perturbation) parts instead of rounded values.
+template <class T, bool JUMPS = false>
+MLAU_HD void flux_mlau(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *f, T jp = T(0),
+                       T jv = T(0))
 {
     const T EPS = T(1e-8);
     const T rol = L[0], vnl = L[1], vtl = L[2], vul = L[3], btl = L[4], bul = L[5], prl = L[6];
@@ -440,7 +462,9 @@ MLAU_HD void flux_mlau(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *
     }
     T mnc = ffl + ffr;
     T mflux = mnc * cfn;
-    mflux -= vmax(T(1.0) - tabs(mnc), T(0)) * theta * cfni * (ptr - ptl) / (rol + ror);
+    const T dpt = JUMPS ? jp : (ptr - ptl);
+    const T dvn = JUMPS ? jv : (vnr - vnl);
+    mflux -= vmax(T(1.0) - tabs(mnc), T(0)) * theta * cfni * dpt / (rol + ror);
     T dir = (mflux > T(0)) ? T(1.0) : T(-1.0);
     T dirl = T(0.5) * (T(1.0) + dir);
     T dirr = T(1.0) - dirl;
@@ -449,7 +473,7 @@ MLAU_HD void flux_mlau(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *
     T mfr = mflux - mfl;
     T ptot = bfl * ptl + bfr * ptr;
     T cfmod = tsqrt(vmax(ccl2, ccr2));
-    ptot -= T(0.25) * bfl * bfr * (rol + ror) * cfmod * (vnr - vnl);
+    ptot -= T(0.25) * bfl * bfr * (rol + ror) * cfmod * dvn;
     ptot -= T(0.5) * (T(1.0) - cfmod * cfni) * (bfl + bfr - T(1.0)) * (ptl + ptr);
     T slvl = sl - vnl, srvr = sr - vnr;
     T snc = dirl * sl + dirr * sr;
@@ -524,8 +548,9 @@ MLAU_HD void flux_mlau(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *
 
 // calc_flux_hlld (mhd_flux.h:456-582, LOWDISS=false) and calc_flux_lhlld
 // (mhd_flux.h:584-719, LOWDISS=true).
-template <class T, bool LOWDISS>
-MLAU_HD void flux_hlld(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *f)
+template <class T, bool LOWDISS, bool JUMPS = false>
+MLAU_HD void flux_hlld(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *f, T jp = T(0),
+                       T jv = T(0))
 {
     const T EPS = T(1e-8);
     const T rol = L[0], vnl = L[1], vtl = L[2], vul = L[3], btl = L[4], bul = L[5], prl = L[6];
@@ -561,8 +586,13 @@ MLAU_HD void flux_hlld(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *
         rslvl = rol * slvl;
         rsrvr = ror * srvr;
         drsvi = T(1.0) / (rsrvr - rslvl);
-        vnc = (rsrvr * vnr - rslvl * vnl - ptr + ptl) * drsvi;
-        ptc = (rsrvr * ptl - rslvl * ptr + rsrvr * rslvl * (vnr - vnl)) * drsvi;
+        if (JUMPS) {
+            vnc = (rsrvr * vnr - rslvl * vnl - jp) * drsvi;
+            ptc = (rsrvr * ptl - rslvl * ptr + rsrvr * rslvl * jv) * drsvi;
+        } else {
+            vnc = (rsrvr * vnr - rslvl * vnl - ptr + ptl) * drsvi;
+            ptc = (rsrvr * ptl - rslvl * ptr + rsrvr * rslvl * (vnr - vnl)) * drsvi;
+        }
     } else {
         cbl2 = vl2 + cal2 + T(2.0) * pml * roli;
         cbr2 = vr2 + car2 + T(2.0) * pmr * rori;
@@ -579,9 +609,10 @@ MLAU_HD void flux_hlld(const T *L, const T *R, T bnc, T gamma, T dv0, T dv1, T *
         T theta = vmin(T(1.0), (cmax - vmin(dv0, T(0.0))) / (cmax - vmin(dv1, T(0.0))));
         theta *= theta;
         theta *= theta;
-        vnc = (rsrvr * vnr - rslvl * vnl - theta * (ptr - ptl)) * drsvi;
+        vnc = (rsrvr * vnr - rslvl * vnl - theta * (JUMPS ? jp : (ptr - ptl))) * drsvi;
         T mcc = vmin(T(1.0), tsqrt(vmax(ccl2, ccr2)) / cmax);
-        ptc = (rsrvr * ptl - rslvl * ptr + (mcc * (T(2.0) - mcc)) * rsrvr * rslvl * (vnr - vnl))
+        ptc = (rsrvr * ptl - rslvl * ptr
+               + (mcc * (T(2.0) - mcc)) * rsrvr * rslvl * (JUMPS ? jv : (vnr - vnl)))
               * drsvi;
     }
     T slvc = sl - vnc, srvc = sr - vnc;
@@ -824,6 +855,20 @@ MLAU_HD void riemann(int which, const T *L, const T *R, T bn, T gamma, T dv0, T 
     case FLUX_MLAU: flux_mlau(L, R, bn, gamma, dv0, dv1, f); break;
     case FLUX_LHLLD: flux_hlld<T, true>(L, R, bn, gamma, dv0, dv1, f); break;
     case FLUX_HLLD: flux_hlld<T, false>(L, R, bn, gamma, dv0, dv1, f); break;
+    default: flux_roe(L, R, bn, gamma, f); break;
+    }
+}
+
+// Riemann solver with caller-formed jumps (FP32-split mode); Roe has no
+// jump-compensated form and uses the rounded face states.
+template <class T>
+MLAU_HD void riemann_jumps(int which, const T *L, const T *R, T bn, T gamma, T dv0, T dv1, T *f,
+                           T jp, T jv)
+{
+    switch (which) {
+    case FLUX_MLAU: flux_mlau<T, true>(L, R, bn, gamma, dv0, dv1, f, jp, jv); break;
+    case FLUX_LHLLD: flux_hlld<T, true, true>(L, R, bn, gamma, dv0, dv1, f, jp, jv); break;
+    case FLUX_HLLD: flux_hlld<T, false, true>(L, R, bn, gamma, dv0, dv1, f, jp, jv); break;
     default: flux_roe(L, R, bn, gamma, f); break;
     }
 }

@@ -1,9 +1,448 @@
-// FP32-split 3D step (placeholder until the split kernels land).
+// FP32-split 3D step.  Same scheme and data layout as the plain FP64 step
+// (3D/MPI/OTvortex/mhd_fd_ct_3d.c), with the arithmetic split by what needs
+// FP64:
+//
+//   FP64  conserved state, its RK3 accumulation of flux differences, primitive
+//         recovery p = (gamma-1)(E - rho v^2/2 - B^2/2) (cancellation at low
+//         Mach and low beta), the CT curl update of face B (div B at round-off).
+//   FP32  characteristic reconstruction and the Riemann solver, the edge EMFs,
+//         the CT weights and shock sensors.
+//
+// Reconstruction works on perturbations from the cell centre: q_m - q_c is
+// formed in FP64 and only then rounded to FP32, and WCNS/MUSCL/linear weights
+// are translation invariant, so the face states keep FP32 relative accuracy in
+// the perturbation, not in the absolute value.  The Riemann solver receives
+// its total-pressure and normal-velocity jumps formed the same way (centre
+// difference in FP64 + perturbation difference in FP32).
+//
+// Kernels per RK stage: prim (FP64), aux (FP32 out), one fused
+// reconstruction + flux kernel per direction (shared-memory tile: each thread
+// reconstructs one cell, then each face thread solves one Riemann problem),
+// emf (FP32), update (FP64 RK combine + CT curl + periodic ghost images).
 #include "sim.cuh"
+#include "point.cuh"
 
 namespace mlau {
-struct SplitFields {};
-int split3d_alloc(Sim *) { set_error("FP32-split mode is not built yet"); return MLAU_ERR_ARG; }
-int split3d_step(Sim *, double) { set_error("FP32-split mode is not built yet"); return MLAU_ERR_ARG; }
-void split3d_free(Sim *) {}
+
+struct SplitFields {
+    float *F[3][7];
+    float *FC[3][2];
+    float *e[3];
+    float *m2;
+    float *ct[3];
+    float *dv[3];
+};
+
+namespace {
+
+struct Dims {
+    int nx, ny, nz, ox, oy, oz;
+    __device__ __forceinline__ long long at(int i, int j, int k) const
+    {
+        return (long long)nx * ((long long)ny * k + j) + i;
+    }
+};
+
+// --- primitives (FP64) -----------------------------------------------------
+__global__ void __launch_bounds__(256)
+ks_prim(PlainFields f, SplitFields g, Dims d, int odr, double gamma)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= d.nx) return;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
+    const double *bx = f.s[5], *by = f.s[6], *bz = f.s[7];
+    const double cx = face2cen(odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
+    const double cy = face2cen(odr, by[w - sy], by[w], by[w + sy], by[w + 2 * sy]);
+    const double cz = face2cen(odr, bz[w - sz], bz[w], bz[w + sz], bz[w + 2 * sz]);
+    const long long s = d.at(i, j, k);
+    const double ro = f.s[0][s];
+    const double iro = 1.0 / ro;
+    const double vx = f.s[1][s] * iro, vy = f.s[2][s] * iro, vz = f.s[3][s] * iro;
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    const double b2 = cx * cx + cy * cy + cz * cz;
+    const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * (ro * v2 + b2));
+    f.vx[s] = vx;
+    f.vy[s] = vy;
+    f.vz[s] = vz;
+    f.pr[s] = pr;
+    f.cx[s] = cx;
+    f.cy[s] = cy;
+    f.cz[s] = cz;
+    g.m2[s] = (float)(v2 / (gamma * pr * iro));
+}
+
+// --- CT weights and shock sensors (FP32 results) ---------------------------
+__device__ __forceinline__ float ct_w(const double *va, const double *vb, const double *ro,
+                                      const double *ba, const double *bbf, long long s,
+                                      long long P, long long Q, long long oa, long long ob)
+{
+    const float eps = 1e-6f;
+    float a = (float)(0.25 * (va[s - P - Q] + va[s - P] + va[s - Q] + va[s]));
+    float c = (float)(0.25 * (vb[s - P - Q] + vb[s - P] + vb[s - Q] + vb[s]));
+    float rc = (float)(0.25 * (ro[s - P - Q] + ro[s - P] + ro[s - Q] + ro[s]));
+    rc = rsqrtf(rc);
+    float fa = (float)(0.5 * (ba[s - oa] + ba[s]));
+    float fb = (float)(0.5 * (bbf[s - ob] + bbf[s]));
+    a = fabsf(a) + fabsf(fa * rc);
+    c = fabsf(c) + fabsf(fb * rc);
+    return (a + 0.5f * eps) / (a + c + eps);
+}
+
+__global__ void __launch_bounds__(256) ks_aux(PlainFields f, SplitFields g, Dims d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= d.nx) return;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    const long long s = d.at(i, j, k);
+    const double *ro = f.s[0];
+    g.ct[0][s] = (i >= 1 && j >= 1) ? ct_w(f.vx, f.vy, ro, f.s[5], f.s[6], s, sy, 1, sy, 1) : 0.5f;
+    g.ct[1][s] = (j >= 1 && k >= 1) ? ct_w(f.vy, f.vz, ro, f.s[6], f.s[7], s, sz, sy, sz, sy) : 0.5f;
+    g.ct[2][s] = (k >= 1 && i >= 1) ? ct_w(f.vz, f.vx, ro, f.s[7], f.s[5], s, sz, 1, 1, sz) : 0.5f;
+    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
+    g.dv[0][s] = (float)vmin((f.vx[w + 1] - f.vx[w]), (f.vx[w] - f.vx[w - 1]));
+    g.dv[1][s] = (float)vmin((f.vy[w + sy] - f.vy[w]), (f.vy[w] - f.vy[w - sy]));
+    g.dv[2][s] = (float)vmin((f.vz[w + sz] - f.vz[w]), (f.vz[w] - f.vz[w - sz]));
+}
+
+// --- fused reconstruction + Riemann flux along axis D ----------------------
+struct View {
+    const double *vn, *vt, *vu, *cn, *ct, *cu, *bface;
+    const float *dvt, *dvu;
+};
+
+// Tile: TA threads along the fast (x) axis x TB along the second axis.  For
+// D=0 the sweep runs along x (TA cells per tile, TB rows); for D=1,2 it runs
+// along the second axis (TB cells per tile, TA columns of x).  A tile of T
+// cells yields T-1 faces; consecutive tiles overlap by one cell.
+template <int D> struct Tile;
+template <> struct Tile<0> { static constexpr int TA = 32, TB = 4; };
+template <> struct Tile<1> { static constexpr int TA = 16, TB = 16; };
+template <> struct Tile<2> { static constexpr int TA = 16, TB = 16; };
+
+struct CellRec {
+    float l[9];    // state perturbation at the cell's right face (left state of face c+1) + 2 central parts
+    float r[9];    // at its left face (right state of face c) + 2 central parts
+};
+
+template <int D>
+__global__ void __launch_bounds__(Tile<D>::TA *Tile<D>::TB)
+ks_sweep(PlainFields f, SplitFields g, View v, Dims d, int odr, int which, float gamma)
+{
+    constexpr int TA = Tile<D>::TA, TB = Tile<D>::TB;
+    constexpr int T = (D == 0) ? TA : TB;  // cells per tile along the sweep
+    __shared__ CellRec rec[TB][TA];
+    __shared__ double base[7][TB][TA];
+    const int ta = threadIdx.x, tb = threadIdx.y;
+    const int p = (D == 0) ? ta : tb;  // position along the sweep inside the tile
+    int i, j, k, len;
+    long long st;
+    if (D == 0) {
+        len = d.nx;
+        st = 1;
+        i = 2 + blockIdx.x * (T - 1) + ta;
+        const long long row = (long long)blockIdx.y * TB + tb;
+        j = (int)(row % d.ny);
+        k = (int)(row / d.ny);
+        if (row >= (long long)d.ny * d.nz) k = d.nz;  // out of range
+    } else if (D == 1) {
+        len = d.ny;
+        st = d.nx;
+        i = blockIdx.x * TA + ta;
+        j = 2 + blockIdx.y * (T - 1) + tb;
+        k = blockIdx.z;
+    } else {
+        len = d.nz;
+        st = (long long)d.nx * d.ny;
+        i = blockIdx.x * TA + ta;
+        k = 2 + blockIdx.y * (T - 1) + tb;
+        j = blockIdx.z;
+    }
+    const int a = (D == 0) ? i : (D == 1 ? j : k);  // sweep coordinate
+    const bool in_box = i < d.nx && j < d.ny && k < d.nz;
+    const bool do_rec = in_box && a >= 2 && a < len - 2;
+    const long long c = in_box ? d.at(i, j, k) : 0;
+
+    if (do_rec) {
+        double q[7][5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            const long long s = c + st * (m - 2);
+            q[0][m] = f.s[0][s];
+            q[1][m] = v.vn[s];
+            q[2][m] = v.vt[s];
+            q[3][m] = v.vu[s];
+            q[4][m] = v.ct[s];
+            q[5][m] = v.cu[s];
+            q[6][m] = f.pr[s];
+        }
+        float dq[7][5], qc[7];
+        unsigned zero = 0;
+#pragma unroll
+        for (int n = 0; n < 7; n++) {
+            qc[n] = (float)q[n][2];
+            bool z = true;
+#pragma unroll
+            for (int m = 0; m < 5; m++) {
+                dq[n][m] = (float)(q[n][m] - q[n][2]);
+                z = z && (q[n][m] == 0.0);
+            }
+            if (z) zero |= 1u << n;
+            base[n][tb][ta] = q[n][2];
+        }
+        float ul[7], ur[7];
+        const float bnc = (float)v.cn[c];
+        const float mm = fmaxf(g.m2[c - st], fmaxf(g.m2[c], g.m2[c + st]));
+        if (mm >= 1.0f) reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
+        else reconst_alfven_core(odr, dq, qc, bnc, gamma, ul, ur);
+#pragma unroll
+        for (int n = 1; n <= 5; n++)
+            if (zero & (1u << n)) { ul[n] = 0.f; ur[n] = 0.f; }
+        CellRec &R = rec[tb][ta];
+#pragma unroll
+        for (int n = 0; n < 7; n++) { R.l[n] = ul[n]; R.r[n] = ur[n]; }
+        // central parts of the two tangential B fluxes: lin(bt vn) - bn_face lin(vt)
+        const double bl = v.bface[c + st], br = v.bface[c];
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            const int kb = 4 + t, kv = 2 + t;
+            const double a0 = q[kb][2] * q[1][2], v0 = q[kv][2];
+            float da[5], dv5[5];
+#pragma unroll
+            for (int m = 0; m < 5; m++) {
+                da[m] = (float)(q[kb][m] * q[1][m] - a0);
+                dv5[m] = (float)(q[kv][m] - v0);
+            }
+            const double al = a0 + (double)lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
+            const double ar = a0 + (double)lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
+            const double vl = v0 + (double)lin_l(odr, dv5[0], dv5[1], dv5[2], dv5[3], dv5[4]);
+            const double vr = v0 + (double)lin_r(odr, dv5[0], dv5[1], dv5[2], dv5[3], dv5[4]);
+            R.l[7 + t] = (float)(al - bl * vl);
+            R.r[7 + t] = (float)(ar - br * vr);
+        }
+    }
+    __syncthreads();
+
+    if (!in_box || p == 0 || a < 3 || a >= len - 2) return;
+    const int tbl = (D == 0) ? tb : tb - 1, tal = (D == 0) ? ta - 1 : ta;
+    const CellRec &RL = rec[tbl][tal];
+    const CellRec &RR = rec[tb][ta];
+    float L[7], Rr[7];
+#pragma unroll
+    for (int n = 0; n < 7; n++) {
+        L[n] = (float)base[n][tbl][tal] + RL.l[n];
+        Rr[n] = (float)base[n][tb][ta] + RR.r[n];
+    }
+    // jumps from split parts: centre difference in FP64, perturbations in FP32
+    auto jump = [&](int n) {
+        return (float)(base[n][tb][ta] - base[n][tbl][tal]) + (RR.r[n] - RL.l[n]);
+    };
+    const float jv = jump(1);
+    const float jp = jump(6) + 0.5f * (jump(4) * (Rr[4] + L[4]) + jump(5) * (Rr[5] + L[5]));
+    const float bn = (float)v.bface[c];
+    const float dv0 = (float)(v.vn[c] - v.vn[c - st]);
+    const float dvtm = fminf(fminf(v.dvt[c - st], v.dvt[c]), fminf(v.dvu[c - st], v.dvu[c]));
+    float F[7];
+    riemann_jumps(which, L, Rr, bn, gamma, dv0, dvtm, F, jp, jv);
+    const float fct = 0.5f * (RL.l[7] + RR.r[7]);
+    const float fcu = 0.5f * (RL.l[8] + RR.r[8]);
+    F[4] -= fct;
+    F[5] -= fcu;
+#pragma unroll
+    for (int n = 0; n < 7; n++) g.F[D][n][c] = F[n];
+    g.FC[D][0][c] = fct;
+    g.FC[D][1][c] = fcu;
+}
+
+// --- edge EMFs (FP32) --------------------------------------------------------
+__device__ __forceinline__ float emf_part32(const float *fu, const float *fc, float w, float h,
+                                            long long c, long long st, int odr)
+{
+    const float ul0 = lin_l(odr, fu[c - 3 * st], fu[c - 2 * st], fu[c - st], fu[c], fu[c + st]);
+    const float ul1 = lin_l(odr, fc[c - 3 * st], fc[c - 2 * st], fc[c - st], fc[c], fc[c + st]);
+    const float ur0 = lin_r(odr, fu[c - 2 * st], fu[c - st], fu[c], fu[c + st], fu[c + 2 * st]);
+    const float ur1 = lin_r(odr, fc[c - 2 * st], fc[c - st], fc[c], fc[c + st], fc[c + 2 * st]);
+    return h * ((ul0 + ur0) + w * (ul1 + ur1));
+}
+
+__global__ void __launch_bounds__(256) ks_emf(SplitFields g, Dims d, int odr)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= d.nx) return;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    const long long c = d.at(i, j, k);
+    const bool xi = (i >= 3 && i < d.nx - 2), yj = (j >= 3 && j < d.ny - 2),
+               zk = (k >= 3 && k < d.nz - 2);
+    float ez = 0.f, ex = 0.f, ey = 0.f;
+    if (xi && yj) {
+        const float w = g.ct[0][c];
+        ez = emf_part32(g.F[0][4], g.FC[0][0], 1.f - w, -0.5f, c, sy, odr)
+             + emf_part32(g.F[1][5], g.FC[1][1], w, 0.5f, c, 1, odr);
+    }
+    if (yj && zk) {
+        const float w = g.ct[1][c];
+        ex = emf_part32(g.F[1][4], g.FC[1][0], 1.f - w, -0.5f, c, sz, odr)
+             + emf_part32(g.F[2][5], g.FC[2][1], w, 0.5f, c, sy, odr);
+    }
+    if (zk && xi) {
+        const float w = g.ct[2][c];
+        ey = emf_part32(g.F[0][5], g.FC[0][1], w, 0.5f, c, sz, odr)
+             + emf_part32(g.F[2][4], g.FC[2][0], 1.f - w, -0.5f, c, 1, odr);
+    }
+    g.e[0][c] = ex;
+    g.e[1][c] = ey;
+    g.e[2][c] = ez;
+}
+
+// --- RK combine + CT curl (FP64) ----------------------------------------------
+__device__ __forceinline__ double df32(int odr, const float *f, long long s, long long st)
+{
+    return fdiff(odr, (double)f[s - st], (double)f[s], (double)f[s + st], (double)f[s + 2 * st]);
+}
+
+__global__ void __launch_bounds__(256)
+ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, double dtdx,
+          double dtdy, double dtdz)
+{
+    const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = d.oy + blockIdx.y, k = d.oz + blockIdx.z;
+    if (i >= d.nx - d.ox) return;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    const long long s = d.at(i, j, k);
+    const int cX[5] = {0, 1, 2, 3, 6}, cY[5] = {0, 3, 1, 2, 6}, cZ[5] = {0, 2, 3, 1, 6};
+    double out[8];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        const double d0 = df32(odr, g.F[0][cX[v]], s, 1);
+        const double d1 = df32(odr, g.F[1][cY[v]], s, sy);
+        const double d2 = df32(odr, g.F[2][cZ[v]], s, sz);
+        out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - dtdx * d0 - dtdy * d1 - dtdz * d2);
+    }
+    out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - dtdy * df32(odr, g.e[2], s, sy)
+                                     + dtdz * df32(odr, g.e[1], s, sz));
+    out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - dtdz * df32(odr, g.e[0], s, sz)
+                                     + dtdx * df32(odr, g.e[2], s, 1));
+    out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - dtdx * df32(odr, g.e[1], s, 1)
+                                     + dtdy * df32(odr, g.e[0], s, sy));
+    const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
+    const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
+    const int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
+    const int ks[3] = {k, k < 2 * d.oz ? k + Nz : -1, k >= Nz ? k - Nz : -1};
+    for (int cc = 0; cc < 3; cc++) {
+        if (ks[cc] < 0) continue;
+        for (int bb = 0; bb < 3; bb++) {
+            if (js[bb] < 0) continue;
+            for (int aa = 0; aa < 3; aa++) {
+                if (is[aa] < 0) continue;
+                const long long t = d.at(is[aa], js[bb], ks[cc]);
+#pragma unroll
+                for (int v = 0; v < 8; v++) f.s[v][t] = out[v];
+            }
+        }
+    }
+}
+
+View make_view(const PlainFields &f, const SplitFields &g, int D)
+{
+    if (D == 0) return {f.vx, f.vy, f.vz, f.cx, f.cy, f.cz, f.s[5], g.dv[1], g.dv[2]};
+    if (D == 1) return {f.vy, f.vz, f.vx, f.cy, f.cz, f.cx, f.s[6], g.dv[2], g.dv[0]};
+    return {f.vz, f.vx, f.vy, f.cz, f.cx, f.cy, f.s[7], g.dv[0], g.dv[1]};
+}
+
+int falloc(Sim *s, float **p, long long n)
+{
+    double *q = nullptr;
+    int rc = dalloc(s, &q, (n + 1) / 2);
+    *p = (float *)q;
+    return rc;
+}
+
+}  // namespace
+
+int split3d_alloc(Sim *s)
+{
+    if (s->g.dim != 3) { set_error("FP32-split mode is 3D only"); return MLAU_ERR_ARG; }
+    PlainFields &f = s->f;
+    const long long n = s->g.n;
+    int rc = 0;
+    for (int v = 0; v < 8; v++) rc |= dalloc(s, &f.s[v], n) | dalloc(s, &f.u0[v], n);
+    double **singles[] = {&f.vx, &f.vy, &f.vz, &f.pr, &f.cx, &f.cy, &f.cz};
+    for (auto p : singles) rc |= dalloc(s, p, n);
+    s->sp = new SplitFields();
+    SplitFields &g = *s->sp;
+    for (int D = 0; D < 3; D++) {
+        for (int v = 0; v < 7; v++) rc |= falloc(s, &g.F[D][v], n);
+        rc |= falloc(s, &g.FC[D][0], n) | falloc(s, &g.FC[D][1], n);
+        rc |= falloc(s, &g.e[D], n) | falloc(s, &g.ct[D], n) | falloc(s, &g.dv[D], n);
+    }
+    rc |= falloc(s, &g.m2, n);
+    return rc ? MLAU_ERR_NOMEM : MLAU_OK;
+}
+
+void split3d_free(Sim *s)
+{
+    delete s->sp;
+    s->sp = nullptr;
+}
+
+int split3d_step(Sim *s, double dt)
+{
+    const Geometry &G = s->g;
+    PlainFields &f = s->f;
+    SplitFields &g = *s->sp;
+    cudaStream_t st = s->stream;
+    const Dims d{G.nx, G.ny, G.nz, G.ox, G.oy, G.oz};
+    {
+        TimedLaunch tl(&s->timer, KK_COPY);
+        for (int v = 0; v < 8; v++)
+            MLAU_CUDA(cudaMemcpyAsync(f.u0[v], f.s[v], sizeof(double) * G.n,
+                                      cudaMemcpyDeviceToDevice, st));
+    }
+    const dim3 cb(128), cg(blocks_for(G.nx, 128), G.ny, G.nz);
+    const dim3 ug(blocks_for(G.nx - 2 * G.ox, 128), G.ny - 2 * G.oy, G.nz - 2 * G.oz);
+    const float gam = (float)s->gamma;
+    for (int rk = 0; rk < s->nrk; rk++) {
+        const double t[3][2] = {{0.0, 1.0},
+                                {0.5 + (s->nrk - 2) * 0.25, 0.5 - (s->nrk - 2) * 0.25},
+                                {1. / 3., 2. / 3.}};
+        const double ra = t[rk][0], rb = t[rk][1];
+        {
+            TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
+            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, s->gamma);
+            ks_aux<<<cg, cb, 0, st>>>(f, g, d);
+        }
+        {
+            TimedLaunch tl(&s->timer, KK_SPLIT_SWEEP);
+            {
+                constexpr int T = Tile<0>::TA;
+                dim3 b(Tile<0>::TA, Tile<0>::TB);
+                dim3 gr(blocks_for(G.nx - 5, T - 1), blocks_for((long long)G.ny * G.nz, Tile<0>::TB));
+                ks_sweep<0><<<gr, b, 0, st>>>(f, g, make_view(f, g, 0), d, s->odr, s->flux, gam);
+            }
+            {
+                constexpr int T = Tile<1>::TB;
+                dim3 b(Tile<1>::TA, Tile<1>::TB);
+                dim3 gr(blocks_for(G.nx, Tile<1>::TA), blocks_for(G.ny - 5, T - 1), G.nz);
+                ks_sweep<1><<<gr, b, 0, st>>>(f, g, make_view(f, g, 1), d, s->odr, s->flux, gam);
+            }
+            {
+                constexpr int T = Tile<2>::TB;
+                dim3 b(Tile<2>::TA, Tile<2>::TB);
+                dim3 gr(blocks_for(G.nx, Tile<2>::TA), blocks_for(G.nz - 5, T - 1), G.ny);
+                ks_sweep<2><<<gr, b, 0, st>>>(f, g, make_view(f, g, 2), d, s->odr, s->flux, gam);
+            }
+        }
+        {
+            TimedLaunch tl(&s->timer, KK_EMF);
+            ks_emf<<<cg, cb, 0, st>>>(g, d, s->odr);
+        }
+        {
+            TimedLaunch tl(&s->timer, KK_SPLIT_UPDATE);
+            ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, ra, rb, dt / G.dx, dt / G.dy, dt / G.dz);
+        }
+        MLAU_CUDA(cudaGetLastError());
+    }
+    return MLAU_OK;
+}
+
 }  // namespace mlau

@@ -38,15 +38,33 @@ def _modes(rng, ndim, nmodes, kmax):
     return np.array(out, dtype=np.int64)
 
 
-def _field(rng, coords, nmodes, kmax, slope=-2.0):
-    """Sum of random-phase cosine modes, amplitude ~ |k|^slope, on `coords`
-    (tuple of broadcastable coordinate arrays in [0,1))."""
-    ks = _modes(rng, len(coords), nmodes, kmax)
+def _trig(k, ph, axes):
+    """cos and sin of 2*pi*k.x + ph on the tensor grid of 1D coordinate
+    vectors `axes` = (x, y[, z]), returned with array axes ordered (z, y, x),
+    built by angle addition from 1D factors (no full-grid transcendental)."""
+    c = s = None
+    for kc, ax in zip(k, axes):
+        a = 2.0 * np.pi * float(kc) * ax
+        ca, sa = np.cos(a), np.sin(a)
+        if c is None:
+            c, s = ca * np.cos(ph) - sa * np.sin(ph), sa * np.cos(ph) + ca * np.sin(ph)
+        else:
+            # prepend a new (slower) array axis for this coordinate
+            shp = (-1,) + (1,) * c.ndim
+            ca, sa = ca.reshape(shp), sa.reshape(shp)
+            c, s = ca * c - sa * s, sa * c + ca * s
+    return c, s
+
+
+def _field(rng, axes, nmodes, kmax, slope=-2.0):
+    """Sum of random-phase cosine modes, amplitude ~ |k|^slope, on the tensor
+    grid of 1D coordinate vectors `axes` (x first)."""
+    ks = _modes(rng, len(axes), nmodes, kmax)
     phases = rng.uniform(0.0, 2.0 * np.pi, size=nmodes)
     f = 0.0
     for k, ph in zip(ks, phases):
-        arg = sum(2.0 * np.pi * float(kc) * c for kc, c in zip(k, coords)) + ph
-        f = f + (float(np.sqrt((k * k).sum())) ** slope) * np.cos(arg)
+        c, _ = _trig(k, ph, axes)
+        f = f + (float(np.sqrt((k * k).sum())) ** slope) * c
     return f
 
 
@@ -90,38 +108,34 @@ def turbulence_3d(n=64, mach=1e-2, seed=0, off=4, gamma=5.0 / 3.0, odr=4, ny=Non
     jc = (np.arange(ny) + 0.5) / ny
     kc = (np.arange(nz) + 0.5) / nz
     ifc, jfc, kfc = np.arange(nx) / nx, np.arange(ny) / ny, np.arange(nz) / nz
-    Z, Y, X = np.meshgrid(kc, jc, ic, indexing="ij")
     B0 = np.array(b0, dtype=np.float64)
     b0abs = float(np.sqrt((B0 * B0).sum()))
     p0 = beta * 0.5 * b0abs ** 2
 
     # density: 1 + 1% random-phase perturbation with |k|<=6
-    dr = _field(rng, (X, Y, Z), nmodes, 6)
+    dr = _field(rng, (ic, jc, kc), nmodes, 6)
     ro = 1.0 + rho_pert * dr / np.sqrt(np.mean(dr * dr))
 
     # solenoidal velocity: v = curl(psi), analytic per mode
     cs = np.sqrt(gamma * p0 / 1.0)
-    v = [np.zeros_like(X) for _ in range(3)]
+    v = [np.zeros((nz, ny, nx)) for _ in range(3)]
     ks = _modes(rng, 3, nmodes, 8)
     for k in ks:
         amp = rng.normal(size=3) * float(np.sqrt((k * k).sum())) ** -2.0
         ph = rng.uniform(0, 2 * np.pi)
-        arg = 2 * np.pi * (k[0] * X + k[1] * Y + k[2] * Z) + ph
-        s = -2 * np.pi * np.sin(arg)
+        _, sn = _trig(k, ph, (ic, jc, kc))
+        sn = -2 * np.pi * sn
         kxp = np.cross(k.astype(np.float64), amp)  # k x psi_k
         for c in range(3):
-            v[c] = v[c] + kxp[c] * s
+            v[c] = v[c] + kxp[c] * sn
     vr = np.sqrt(np.mean(v[0] ** 2 + v[1] ** 2 + v[2] ** 2))
     v = [c * (mach * cs / vr) for c in v]
 
     # vector potential on edges: Ax at (i, j-1/2, k-1/2), Ay at (i-1/2, j, k-1/2),
     # Az at (i-1/2, j-1/2, k); B = B0 + curl A on faces with the scheme difference
-    Zax, Yax, Xax = np.meshgrid(kfc, jfc, ic, indexing="ij")
-    Zay, Yay, Xay = np.meshgrid(kfc, jc, ifc, indexing="ij")
-    Zaz, Yaz, Xaz = np.meshgrid(kc, jfc, ifc, indexing="ij")
-    fa = [_field(rng, (Xax, Yax, Zax), nmodes, 6),
-          _field(rng, (Xay, Yay, Zay), nmodes, 6),
-          _field(rng, (Xaz, Yaz, Zaz), nmodes, 6)]
+    fa = [_field(rng, (ic, jfc, kfc), nmodes, 6),
+          _field(rng, (ifc, jc, kfc), nmodes, 6),
+          _field(rng, (ifc, jfc, kc), nmodes, 6)]
     # arrays are (z, y, x): axis 2 = x, 1 = y, 0 = z.  Differences land one
     # half-cell over, matching the face the component lives on.
     bx = _ddx(fa[2], 1, ny, odr) - _ddx(fa[1], 0, nz, odr)
@@ -154,15 +168,13 @@ def turbulence_2d(n=512, seed=0, off=4, gamma=5.0 / 3.0, odr=4, ny=None, vrms=0.
     ic = (np.arange(nx) + 0.5) / nx
     jc = (np.arange(ny) + 0.5) / ny
     ifc, jfc = np.arange(nx) / nx, np.arange(ny) / ny
-    Y, X = np.meshgrid(jc, ic, indexing="ij")
     p0 = 1.0 / gamma
-    vx = _field(rng, (X, Y), nmodes, kmax)
-    vy = _field(rng, (X, Y), nmodes, kmax)
+    vx = _field(rng, (ic, jc), nmodes, kmax)
+    vy = _field(rng, (ic, jc), nmodes, kmax)
     r = np.sqrt(np.mean(vx ** 2 + vy ** 2))
     vx, vy = vx * (vrms / r), vy * (vrms / r)
     # Az at cell corners (i-1/2, j-1/2)
-    Yc, Xc = np.meshgrid(jfc, ifc, indexing="ij")
-    az = _field(rng, (Xc, Yc), nmodes, kmax)
+    az = _field(rng, (ifc, jfc), nmodes, kmax)
     bx = _ddx(az, 0, ny, odr)
     by = -_ddx(az, 1, nx, odr)
     b2 = np.mean(_center(bx, 1, odr) ** 2 + _center(by, 0, odr) ** 2)

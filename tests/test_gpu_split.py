@@ -1,0 +1,76 @@
+"""FP32-split mode against the plain FP64 GPU path on the same inputs.
+
+Tolerance (stated by the workload spec): relative L1 error of density
+<= 1e-6 with respect to the FP64 path; div B stays at round-off because the CT
+curl runs in FP64.  The other variables' L1 errors are checked against looser
+per-variable bounds to catch regressions."""
+import numpy as np
+import pytest
+
+import mlau_gb300 as M
+from mlau_gb300 import ics
+
+pytestmark = pytest.mark.gpu
+
+RHO_L1_TOL = 1e-6
+INT = (slice(4, -4),) * 3
+
+
+def l1_rel(a, b):
+    return float(np.abs(a[INT] - b[INT]).sum() / np.abs(b[INT]).sum())
+
+
+def run(st, m, steps, dt, precision, flux="mlau"):
+    with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"], odr=4, flux=flux,
+               precision=precision) as s:
+        s.upload(st)
+        s.step(dt, steps)
+        return s.download()
+
+
+@pytest.mark.parametrize("mach", (1e-2, 1e-4))
+def test_split_density_l1_vs_fp64(mach):
+    st, m = ics.turbulence_3d(n=32, mach=mach, seed=5)
+    dt = 0.4 * m["dx"] / m["vfast"]
+    ref = run(st, m, 50, dt, M.FP64)
+    got = run(st, m, 50, dt, M.FP32_SPLIT)
+    err = {k: l1_rel(got[k], ref[k]) for k in ("ro", "en", "bx", "by", "bz")}
+    assert err["ro"] <= RHO_L1_TOL, err
+    assert err["en"] <= 1e-6 and max(err["bx"], err["by"], err["bz"]) <= 1e-5, err
+    assert ics.div_b_3d(got, m["dx"], m["dy"], m["dz"]) <= 1e-12
+
+
+@pytest.mark.parametrize("flux", ("mlau", "lhlld", "hlld", "roe"))
+def test_split_all_solvers_supersonic(flux):
+    """Mach ~1: the full 7-wave projection runs; states stay close to FP64."""
+    st, m = ics.turbulence_3d(n=16, mach=1.0, seed=9)
+    dt = 0.3 * m["dx"] / (m["vfast"] + 1.0)
+    ref = run(st, m, 10, dt, M.FP64, flux)
+    got = run(st, m, 10, dt, M.FP32_SPLIT, flux)
+    for k in ("ro", "en"):
+        assert np.isfinite(got[k]).all()
+        assert l1_rel(got[k], ref[k]) <= 1e-5, (k, l1_rel(got[k], ref[k]))
+
+
+def test_split_ghosts_are_periodic_images():
+    st, m = ics.turbulence_3d(n=12, mach=0.1, seed=2)
+    got = run(st, m, 3, 1e-3, M.FP32_SPLIT)
+    for k, a in got.items():
+        inner = a[INT]
+        assert np.array_equal(np.pad(inner, 4, mode="wrap"), a), k
+
+
+def test_split_dropin_driver():
+    st, m = ics.turbulence_3d(n=16, mach=1e-2, seed=4)
+    nz, ny, nx = st["ro"].shape
+    ref = run(st, m, 1, 1e-3, M.FP32_SPLIT)
+    M.set_scheme(3, 4, "mlau", 3)
+    M.set_precision(3, M.FP32_SPLIT)
+    try:
+        M.mhd_fd_ct_3d(*[st[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")], 1e-3,
+                       m["dx"], m["dy"], m["dz"], nx, ny, nz, 4, 4, 4, m["gamma"])
+    finally:
+        M.set_precision(3, M.FP64)
+        M.release_dropin()
+    for k in ref:
+        assert np.array_equal(st[k], ref[k]), k
