@@ -143,6 +143,29 @@ int mlau_sim_launches_per_step(mlau_sim *sim);
 int mlau_sim_time_steps(mlau_sim *sim, double dt, int nsteps, double *ms);
 
 /* ---------------------------------------------------------------------- */
+/* 4. Allocation-free 1D step                                              */
+/* ---------------------------------------------------------------------- */
+/* No counterpart in the reference (its drivers malloc scratch on every call).
+ * For callers that cannot allocate device memory - code inside a host
+ * framework that owns every device allocation, or a service holding a fixed
+ * device-memory budget: one 1D step like mhd_fd4c_1d (odr/flux/nrk/bc as in
+ * the handle API) on arrays the caller already holds in device-accessible
+ * memory, updated in place, with no allocation.  Its scratch is one static
+ * device array of 32*(MLAU_NOALLOC_1D_MAX_NX+1) doubles (4.2 MB) that every
+ * GPU loading the library holds until the process exits; nx above
+ * MLAU_NOALLOC_1D_MAX_NX is rejected.  The first call on a device resolves
+ * that array's device address (cudaGetSymbolAddress) - make it before any
+ * stream capture.  The work is enqueued on `stream` (NULL: the legacy default
+ * stream) and the call returns without waiting.  All calls share the one
+ * array: calls that overlap on the GPU (different streams, no ordering) race
+ * on it.  Nothing in the scratch needs clearing between calls: every element
+ * a step reads is written earlier in the same step. */
+#define MLAU_NOALLOC_1D_MAX_NX 16392
+int mlau_fd4c_1d_noalloc(double *ro, double *mx, double *my, double *mz, double *en, double *by,
+                         double *bz, double bx, double dt, double dx, int nx, int xoff,
+                         double gamma, int odr, int flux, int nrk, int bc, void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* 3. Measurement helpers                                                  */
 /* ---------------------------------------------------------------------- */
 /* FMA throughput of the current device in flop/s (2 flops per FMA), FP64 and

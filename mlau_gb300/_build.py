@@ -33,6 +33,7 @@ UNITS = {
     "split3d.cu": FAST32,
     "api.cu": EXACT,
     "peaks.cu": EXACT,
+    "noalloc1d.cu": EXACT,
     "cxx_linkage.cpp": [],
 }
 

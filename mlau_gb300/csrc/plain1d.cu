@@ -227,3 +227,34 @@ int plain1d_step(Sim *s, double dt)
 }
 
 }  // namespace mlau
+
+namespace mlau {
+
+// Enqueue one 1D step on `st` for caller-provided fields (state and scratch
+// already placed); used by the allocation-free entry point.  Same kernels and
+// launch sequence as plain1d_step.
+int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, int nrk, int bc,
+                    double bx, double dt, double dx, double gamma, cudaStream_t st)
+{
+    const double dtdx = dt / dx;
+    for (int v = 0; v < 8; v++) {
+        if (v == 5) continue;
+        MLAU_CUDA(cudaMemcpyAsync(f.u0[v], f.s[v], sizeof(double) * nx, cudaMemcpyDeviceToDevice,
+                                  st));
+    }
+    const int T = 128;
+    for (int rk = 0; rk < nrk; rk++) {
+        double ra, rb;
+        rk_coef(nrk, rk, ra, rb);
+        k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma);
+        k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, odr, bx, gamma);
+        k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
+        if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<1, 1, 0, st>>>(f, nx, off, bx, dtdx, gamma);
+        k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(f, nx, off, odr, ra, rb, dtdx,
+                                                            bc == MLAU_BC1D_PERIODIC);
+        MLAU_CUDA(cudaGetLastError());
+    }
+    return MLAU_OK;
+}
+
+}  // namespace mlau
