@@ -8,23 +8,31 @@
 //   FP32  characteristic reconstruction and the Riemann solver, the edge EMFs,
 //         the CT weights and shock sensors.
 //
-// Reconstruction works on perturbations from the cell centre: q_m - q_c is
-// formed in FP64 and only then rounded to FP32, and WCNS/MUSCL/linear weights
-// are translation invariant, so the face states keep FP32 relative accuracy in
-// the perturbation, not in the absolute value.  The Riemann solver receives
-// its total-pressure and normal-velocity jumps formed the same way (centre
-// difference in FP64 + perturbation difference in FP32).
+// Reconstruction works on perturbations from the cell centre, q_m - q_c, and
+// WCNS/MUSCL/linear weights are translation invariant, so the face states
+// keep FP32 relative accuracy in the perturbation, not in the absolute value.
+// The Riemann solver receives its total-pressure and normal-velocity jumps
+// formed the same way (centre difference + perturbation difference).
 //
-// Kernels per RK stage: prim (FP64), aux (FP32 out), one fused
-// reconstruction + flux kernel per direction (shared-memory tile: each thread
-// reconstructs one cell, then each face thread solves one Riemann problem),
-// emf (FP32), update (FP64 RK combine + CT curl + periodic ghost images).
+// The primitives leave the FP64 prep kernel as (hi, lo) float pairs with
+// q = hi + lo to ~48 bits, so every later difference q_m - q_c is formed in
+// FP32 as (hi_m - hi_c) + (lo_m - lo_c) without losing the perturbation.
+// Flux differences are formed in FP32 (neighbouring fluxes of one sign
+// subtract exactly) and added to the FP64 state in FP64.
+//
+// Kernels per RK stage: prep (FP64 primitive recovery -> float pairs), aux
+// (FP32 CT weights and shock sensors), one fused reconstruction + flux kernel
+// per direction (shared-memory tile: each thread reconstructs one cell, then
+// each face thread solves one Riemann problem), emf (FP32), update (FP64 RK
+// combine + CT curl + periodic ghost images).
 #include "sim.cuh"
 #include "point.cuh"
 
 namespace mlau {
 
 struct SplitFields {
+    float2 *q[8];    // ro, vx, vy, vz, cx, cy, cz, pr as (hi, lo) pairs
+    float *bf[3];    // face-centred bx, by, bz rounded to FP32
     float *F[3][7];
     float *FC[3][2];
     float *e[3];
@@ -43,7 +51,13 @@ struct Dims {
     }
 };
 
-// --- primitives (FP64) -----------------------------------------------------
+// --- primitives (FP64 recovery, FP32-pair output) ------------------------
+__device__ __forceinline__ float2 split2(double x)
+{
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+
 __global__ void __launch_bounds__(256)
 ks_prim(PlainFields f, SplitFields g, Dims d, int odr, double gamma)
 {
@@ -57,58 +71,76 @@ ks_prim(PlainFields f, SplitFields g, Dims d, int odr, double gamma)
     const double cz = face2cen(odr, bz[w - sz], bz[w], bz[w + sz], bz[w + 2 * sz]);
     const long long s = d.at(i, j, k);
     const double ro = f.s[0][s];
-    const double iro = 1.0 / ro;
-    const double vx = f.s[1][s] * iro, vy = f.s[2][s] * iro, vz = f.s[3][s] * iro;
-    const double v2 = vx * vx + vy * vy + vz * vz;
+    // Velocities and the kinetic energy in FP32: rho v^2/2 enters the pressure
+    // as an additive term, so its FP32 rounding (1e-7 of itself) stays below
+    // the pressure's own FP32 resolution at any Mach number; the cancelling
+    // terms E and B^2/2 stay FP64.
+    const float rof = (float)ro, irof = 1.0f / rof;
+    const float vx = (float)f.s[1][s] * irof, vy = (float)f.s[2][s] * irof,
+                vz = (float)f.s[3][s] * irof;
+    const float v2 = vx * vx + vy * vy + vz * vz;
     const double b2 = cx * cx + cy * cy + cz * cz;
-    const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * (ro * v2 + b2));
-    f.vx[s] = vx;
-    f.vy[s] = vy;
-    f.vz[s] = vz;
-    f.pr[s] = pr;
-    f.cx[s] = cx;
-    f.cy[s] = cy;
-    f.cz[s] = cz;
-    g.m2[s] = (float)(v2 / (gamma * pr * iro));
+    const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * ((double)(rof * v2) + b2));
+    g.q[0][s] = split2(ro);
+    g.q[1][s] = make_float2(vx, 0.f);
+    g.q[2][s] = make_float2(vy, 0.f);
+    g.q[3][s] = make_float2(vz, 0.f);
+    g.q[4][s] = split2(cx);
+    g.q[5][s] = split2(cy);
+    g.q[6][s] = split2(cz);
+    g.q[7][s] = split2(pr);
+    g.bf[0][s] = (float)bx[s];
+    g.bf[1][s] = (float)by[s];
+    g.bf[2][s] = (float)bz[s];
+    g.m2[s] = v2 / ((float)gamma * (float)pr * irof);
 }
 
-// --- CT weights and shock sensors (FP32 results) ---------------------------
-__device__ __forceinline__ float ct_w(const double *va, const double *vb, const double *ro,
-                                      const double *ba, const double *bbf, long long s,
-                                      long long P, long long Q, long long oa, long long ob)
+// --- CT weights and shock sensors (FP32) ----------------------------------
+__device__ __forceinline__ float qf(const float2 *a, long long s) { return a[s].x + a[s].y; }
+// difference a[s] - a[t] from the pairs
+__device__ __forceinline__ float qd(const float2 *a, long long s, long long t)
+{
+    const float2 u = a[s], v = a[t];
+    return (u.x - v.x) + (u.y - v.y);
+}
+
+__device__ __forceinline__ float ct_w(const float2 *va, const float2 *vb, const float2 *ro,
+                                      const float *ba, const float *bbf, long long s, long long P,
+                                      long long Q, long long oa, long long ob)
 {
     const float eps = 1e-6f;
-    float a = (float)(0.25 * (va[s - P - Q] + va[s - P] + va[s - Q] + va[s]));
-    float c = (float)(0.25 * (vb[s - P - Q] + vb[s - P] + vb[s - Q] + vb[s]));
-    float rc = (float)(0.25 * (ro[s - P - Q] + ro[s - P] + ro[s - Q] + ro[s]));
+    float a = 0.25f * (qf(va, s - P - Q) + qf(va, s - P) + qf(va, s - Q) + qf(va, s));
+    float c = 0.25f * (qf(vb, s - P - Q) + qf(vb, s - P) + qf(vb, s - Q) + qf(vb, s));
+    float rc = 0.25f * (qf(ro, s - P - Q) + qf(ro, s - P) + qf(ro, s - Q) + qf(ro, s));
     rc = rsqrtf(rc);
-    float fa = (float)(0.5 * (ba[s - oa] + ba[s]));
-    float fb = (float)(0.5 * (bbf[s - ob] + bbf[s]));
+    const float fa = 0.5f * (ba[s - oa] + ba[s]);
+    const float fb = 0.5f * (bbf[s - ob] + bbf[s]);
     a = fabsf(a) + fabsf(fa * rc);
     c = fabsf(c) + fabsf(fb * rc);
     return (a + 0.5f * eps) / (a + c + eps);
 }
 
-__global__ void __launch_bounds__(256) ks_aux(PlainFields f, SplitFields g, Dims d)
+__global__ void __launch_bounds__(256) ks_aux(SplitFields g, Dims d)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= d.nx) return;
     const long long sy = d.nx, sz = (long long)d.nx * d.ny;
     const long long s = d.at(i, j, k);
-    const double *ro = f.s[0];
-    g.ct[0][s] = (i >= 1 && j >= 1) ? ct_w(f.vx, f.vy, ro, f.s[5], f.s[6], s, sy, 1, sy, 1) : 0.5f;
-    g.ct[1][s] = (j >= 1 && k >= 1) ? ct_w(f.vy, f.vz, ro, f.s[6], f.s[7], s, sz, sy, sz, sy) : 0.5f;
-    g.ct[2][s] = (k >= 1 && i >= 1) ? ct_w(f.vz, f.vx, ro, f.s[7], f.s[5], s, sz, 1, 1, sz) : 0.5f;
+    const float2 *ro = g.q[0], *vx = g.q[1], *vy = g.q[2], *vz = g.q[3];
+    g.ct[0][s] = (i >= 1 && j >= 1) ? ct_w(vx, vy, ro, g.bf[0], g.bf[1], s, sy, 1, sy, 1) : 0.5f;
+    g.ct[1][s] = (j >= 1 && k >= 1) ? ct_w(vy, vz, ro, g.bf[1], g.bf[2], s, sz, sy, sz, sy) : 0.5f;
+    g.ct[2][s] = (k >= 1 && i >= 1) ? ct_w(vz, vx, ro, g.bf[2], g.bf[0], s, sz, 1, 1, sz) : 0.5f;
     const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
-    g.dv[0][s] = (float)vmin((f.vx[w + 1] - f.vx[w]), (f.vx[w] - f.vx[w - 1]));
-    g.dv[1][s] = (float)vmin((f.vy[w + sy] - f.vy[w]), (f.vy[w] - f.vy[w - sy]));
-    g.dv[2][s] = (float)vmin((f.vz[w + sz] - f.vz[w]), (f.vz[w] - f.vz[w - sz]));
+    g.dv[0][s] = fminf(qd(vx, w + 1, w), qd(vx, w, w - 1));
+    g.dv[1][s] = fminf(qd(vy, w + sy, w), qd(vy, w, w - sy));
+    g.dv[2][s] = fminf(qd(vz, w + sz, w), qd(vz, w, w - sz));
 }
 
 // --- fused reconstruction + Riemann flux along axis D ----------------------
+// Rotated views: normal/tangential velocity, cell B (normal, t, u), face B.
 struct View {
-    const double *vn, *vt, *vu, *cn, *ct, *cu, *bface;
-    const float *dvt, *dvu;
+    const float2 *vn, *vt, *vu, *cn, *ct, *cu;
+    const float *bface, *dvt, *dvu;
 };
 
 // Tile: TA threads along the fast (x) axis x TB along the second axis.  For
@@ -120,19 +152,20 @@ template <> struct Tile<0> { static constexpr int TA = 32, TB = 4; };
 template <> struct Tile<1> { static constexpr int TA = 16, TB = 16; };
 template <> struct Tile<2> { static constexpr int TA = 16, TB = 16; };
 
-struct CellRec {
-    float l[9];    // state perturbation at the cell's right face (left state of face c+1) + 2 central parts
-    float r[9];    // at its left face (right state of face c) + 2 central parts
-};
+// Per-cell results in shared memory, stored variable-major ([var][TB][TA]) so
+// that the lanes of a warp touch consecutive words (no bank conflicts):
+//   sl - perturbation at the cell's right face (left state of face c+1) + 2 central parts
+//   sr - at its left face (right state of face c) + 2 central parts
+//   sb - the cell-centre state (ro, vn, vt, vu, bt, bu, pr) as (hi, lo)
 
 template <int D>
 __global__ void __launch_bounds__(Tile<D>::TA *Tile<D>::TB)
-ks_sweep(PlainFields f, SplitFields g, View v, Dims d, int odr, int which, float gamma)
+ks_sweep(SplitFields g, View v, Dims d, int odr, int which, float gamma)
 {
     constexpr int TA = Tile<D>::TA, TB = Tile<D>::TB;
     constexpr int T = (D == 0) ? TA : TB;  // cells per tile along the sweep
-    __shared__ CellRec rec[TB][TA];
-    __shared__ double base[7][TB][TA];
+    __shared__ float sl[9][TB][TA], sr[9][TB][TA];
+    __shared__ float2 sb[7][TB][TA];
     const int ta = threadIdx.x, tb = threadIdx.y;
     const int p = (D == 0) ? ta : tb;  // position along the sweep inside the tile
     int i, j, k, len;
@@ -164,88 +197,77 @@ ks_sweep(PlainFields f, SplitFields g, View v, Dims d, int odr, int which, float
     const long long c = in_box ? d.at(i, j, k) : 0;
 
     if (do_rec) {
-        double q[7][5];
-#pragma unroll
-        for (int m = 0; m < 5; m++) {
-            const long long s = c + st * (m - 2);
-            q[0][m] = f.s[0][s];
-            q[1][m] = v.vn[s];
-            q[2][m] = v.vt[s];
-            q[3][m] = v.vu[s];
-            q[4][m] = v.ct[s];
-            q[5][m] = v.cu[s];
-            q[6][m] = f.pr[s];
-        }
+        const float2 *src[7] = {g.q[0], v.vn, v.vt, v.vu, v.ct, v.cu, g.q[7]};
         float dq[7][5], qc[7];
         unsigned zero = 0;
 #pragma unroll
         for (int n = 0; n < 7; n++) {
-            qc[n] = (float)q[n][2];
+            float2 h[5];
+#pragma unroll
+            for (int m = 0; m < 5; m++) h[m] = src[n][c + st * (m - 2)];
+            qc[n] = h[2].x + h[2].y;
             bool z = true;
 #pragma unroll
             for (int m = 0; m < 5; m++) {
-                dq[n][m] = (float)(q[n][m] - q[n][2]);
-                z = z && (q[n][m] == 0.0);
+                dq[n][m] = (h[m].x - h[2].x) + (h[m].y - h[2].y);
+                z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
             }
             if (z) zero |= 1u << n;
-            base[n][tb][ta] = q[n][2];
+            sb[n][tb][ta] = h[2];
         }
         float ul[7], ur[7];
-        const float bnc = (float)v.cn[c];
+        const float bnc = qf(v.cn, c);
         const float mm = fmaxf(g.m2[c - st], fmaxf(g.m2[c], g.m2[c + st]));
         if (mm >= 1.0f) reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
         else reconst_alfven_core(odr, dq, qc, bnc, gamma, ul, ur);
 #pragma unroll
         for (int n = 1; n <= 5; n++)
             if (zero & (1u << n)) { ul[n] = 0.f; ur[n] = 0.f; }
-        CellRec &R = rec[tb][ta];
 #pragma unroll
-        for (int n = 0; n < 7; n++) { R.l[n] = ul[n]; R.r[n] = ur[n]; }
+        for (int n = 0; n < 7; n++) { sl[n][tb][ta] = ul[n]; sr[n][tb][ta] = ur[n]; }
         // central parts of the two tangential B fluxes: lin(bt vn) - bn_face lin(vt)
-        const double bl = v.bface[c + st], br = v.bface[c];
+        const float bl = v.bface[c + st], br = v.bface[c];
 #pragma unroll
         for (int t = 0; t < 2; t++) {
             const int kb = 4 + t, kv = 2 + t;
-            const double a0 = q[kb][2] * q[1][2], v0 = q[kv][2];
-            float da[5], dv5[5];
+            const float a0 = (qc[kb]) * (qc[1]);
+            float da[5];
 #pragma unroll
-            for (int m = 0; m < 5; m++) {
-                da[m] = (float)(q[kb][m] * q[1][m] - a0);
-                dv5[m] = (float)(q[kv][m] - v0);
-            }
-            const double al = a0 + (double)lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
-            const double ar = a0 + (double)lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
-            const double vl = v0 + (double)lin_l(odr, dv5[0], dv5[1], dv5[2], dv5[3], dv5[4]);
-            const double vr = v0 + (double)lin_r(odr, dv5[0], dv5[1], dv5[2], dv5[3], dv5[4]);
-            R.l[7 + t] = (float)(al - bl * vl);
-            R.r[7 + t] = (float)(ar - br * vr);
+            for (int m = 0; m < 5; m++)
+                da[m] = (qc[kb] + dq[kb][m]) * (qc[1] + dq[1][m]) - a0;
+            const float al = a0 + lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
+            const float ar = a0 + lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
+            const float vl = qc[kv] + lin_l(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
+            const float vr = qc[kv] + lin_r(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
+            sl[7 + t][tb][ta] = al - bl * vl;
+            sr[7 + t][tb][ta] = ar - br * vr;
         }
     }
     __syncthreads();
 
     if (!in_box || p == 0 || a < 3 || a >= len - 2) return;
     const int tbl = (D == 0) ? tb : tb - 1, tal = (D == 0) ? ta - 1 : ta;
-    const CellRec &RL = rec[tbl][tal];
-    const CellRec &RR = rec[tb][ta];
     float L[7], Rr[7];
 #pragma unroll
     for (int n = 0; n < 7; n++) {
-        L[n] = (float)base[n][tbl][tal] + RL.l[n];
-        Rr[n] = (float)base[n][tb][ta] + RR.r[n];
+        L[n] = (sb[n][tbl][tal].x + sb[n][tbl][tal].y) + sl[n][tbl][tal];
+        Rr[n] = (sb[n][tb][ta].x + sb[n][tb][ta].y) + sr[n][tb][ta];
     }
-    // jumps from split parts: centre difference in FP64, perturbations in FP32
+    // jumps from split parts: centre difference from the pairs, plus the
+    // difference of the FP32 perturbations
     auto jump = [&](int n) {
-        return (float)(base[n][tb][ta] - base[n][tbl][tal]) + (RR.r[n] - RL.l[n]);
+        return ((sb[n][tb][ta].x - sb[n][tbl][tal].x) + (sb[n][tb][ta].y - sb[n][tbl][tal].y))
+               + (sr[n][tb][ta] - sl[n][tbl][tal]);
     };
     const float jv = jump(1);
     const float jp = jump(6) + 0.5f * (jump(4) * (Rr[4] + L[4]) + jump(5) * (Rr[5] + L[5]));
-    const float bn = (float)v.bface[c];
-    const float dv0 = (float)(v.vn[c] - v.vn[c - st]);
+    const float bn = v.bface[c];
+    const float dv0 = (sb[1][tb][ta].x - sb[1][tbl][tal].x) + (sb[1][tb][ta].y - sb[1][tbl][tal].y);
     const float dvtm = fminf(fminf(v.dvt[c - st], v.dvt[c]), fminf(v.dvu[c - st], v.dvu[c]));
     float F[7];
     riemann_jumps(which, L, Rr, bn, gamma, dv0, dvtm, F, jp, jv);
-    const float fct = 0.5f * (RL.l[7] + RR.r[7]);
-    const float fcu = 0.5f * (RL.l[8] + RR.r[8]);
+    const float fct = 0.5f * (sl[7][tbl][tal] + sr[7][tb][ta]);
+    const float fcu = 0.5f * (sl[8][tbl][tal] + sr[8][tb][ta]);
     F[4] -= fct;
     F[5] -= fcu;
 #pragma unroll
@@ -294,15 +316,27 @@ __global__ void __launch_bounds__(256) ks_emf(SplitFields g, Dims d, int odr)
     g.e[2][c] = ez;
 }
 
-// --- RK combine + CT curl (FP64) ----------------------------------------------
-__device__ __forceinline__ double df32(int odr, const float *f, long long s, long long st)
+// --- RK combine + CT curl ------------------------------------------------------
+// The flux divergence dt/dx dF + dt/dy dG + dt/dz dH is formed in FP32 (each
+// difference of neighbouring FP32 fluxes is exact when they share sign and
+// magnitude) and accumulated into the FP64 state in FP64.
+__device__ __forceinline__ float df32(int odr, const float *f, long long s, long long st)
 {
-    return fdiff(odr, (double)f[s - st], (double)f[s], (double)f[s + st], (double)f[s + 2 * st]);
+    return fdiff(odr, f[s - st], f[s], f[s + st], f[s + 2 * st]);
+}
+
+// FP64 face-to-centre difference of FP32 edge EMFs; the 1/24 of the 4th-order
+// stencil is a multiplication here (no FP64 division).
+__device__ __forceinline__ double df64(int odr, const float *f, long long s, long long st)
+{
+    const double f0 = f[s - st], f1 = f[s], f2 = f[s + st], f3 = f[s + 2 * st];
+    if (odr <= 2) return f2 - f1;
+    return (27.0 * (f2 - f1) - (f3 - f0)) * (1.0 / 24.0);
 }
 
 __global__ void __launch_bounds__(256)
-ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, double dtdx,
-          double dtdy, double dtdz)
+ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, float dtdx,
+          float dtdy, float dtdz, double dtdx_d, double dtdy_d, double dtdz_d)
 {
     const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = d.oy + blockIdx.y, k = d.oz + blockIdx.z;
@@ -313,17 +347,20 @@ ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, d
     double out[8];
 #pragma unroll
     for (int v = 0; v < 5; v++) {
-        const double d0 = df32(odr, g.F[0][cX[v]], s, 1);
-        const double d1 = df32(odr, g.F[1][cY[v]], s, sy);
-        const double d2 = df32(odr, g.F[2][cZ[v]], s, sz);
-        out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - dtdx * d0 - dtdy * d1 - dtdz * d2);
+        const float div = dtdx * df32(odr, g.F[0][cX[v]], s, 1) + dtdy * df32(odr, g.F[1][cY[v]], s, sy)
+                          + dtdz * df32(odr, g.F[2][cZ[v]], s, sz);
+        out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - (double)div);
     }
-    out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - dtdy * df32(odr, g.e[2], s, sy)
-                                     + dtdz * df32(odr, g.e[1], s, sz));
-    out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - dtdz * df32(odr, g.e[0], s, sz)
-                                     + dtdx * df32(odr, g.e[2], s, 1));
-    out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - dtdx * df32(odr, g.e[1], s, 1)
-                                     + dtdy * df32(odr, g.e[0], s, sy));
+    // CT curl in FP64: the differences of the FP32 edge EMFs are exact in
+    // FP64, so the discrete divergence of the B increment cancels to FP64
+    // round-off (in FP32, 27*(E2-E1) alone would need more than 24 bits).
+    const double ddx = (double)dtdx_d, ddy = (double)dtdy_d, ddz = (double)dtdz_d;
+    out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - ddy * df64(odr, g.e[2], s, sy)
+                                     + ddz * df64(odr, g.e[1], s, sz));
+    out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - ddz * df64(odr, g.e[0], s, sz)
+                                     + ddx * df64(odr, g.e[2], s, 1));
+    out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - ddx * df64(odr, g.e[1], s, 1)
+                                     + ddy * df64(odr, g.e[0], s, sy));
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
     const int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -342,11 +379,11 @@ ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, d
     }
 }
 
-View make_view(const PlainFields &f, const SplitFields &g, int D)
+View make_view(const SplitFields &g, int D)
 {
-    if (D == 0) return {f.vx, f.vy, f.vz, f.cx, f.cy, f.cz, f.s[5], g.dv[1], g.dv[2]};
-    if (D == 1) return {f.vy, f.vz, f.vx, f.cy, f.cz, f.cx, f.s[6], g.dv[2], g.dv[0]};
-    return {f.vz, f.vx, f.vy, f.cz, f.cx, f.cy, f.s[7], g.dv[0], g.dv[1]};
+    if (D == 0) return {g.q[1], g.q[2], g.q[3], g.q[4], g.q[5], g.q[6], g.bf[0], g.dv[1], g.dv[2]};
+    if (D == 1) return {g.q[2], g.q[3], g.q[1], g.q[5], g.q[6], g.q[4], g.bf[1], g.dv[2], g.dv[0]};
+    return {g.q[3], g.q[1], g.q[2], g.q[6], g.q[4], g.q[5], g.bf[2], g.dv[0], g.dv[1]};
 }
 
 int falloc(Sim *s, float **p, long long n)
@@ -366,10 +403,10 @@ int split3d_alloc(Sim *s)
     const long long n = s->g.n;
     int rc = 0;
     for (int v = 0; v < 8; v++) rc |= dalloc(s, &f.s[v], n) | dalloc(s, &f.u0[v], n);
-    double **singles[] = {&f.vx, &f.vy, &f.vz, &f.pr, &f.cx, &f.cy, &f.cz};
-    for (auto p : singles) rc |= dalloc(s, p, n);
     s->sp = new SplitFields();
     SplitFields &g = *s->sp;
+    for (int v = 0; v < 8; v++) rc |= dalloc(s, (double **)&g.q[v], n);
+    for (int D = 0; D < 3; D++) rc |= falloc(s, &g.bf[D], n);
     for (int D = 0; D < 3; D++) {
         for (int v = 0; v < 7; v++) rc |= falloc(s, &g.F[D][v], n);
         rc |= falloc(s, &g.FC[D][0], n) | falloc(s, &g.FC[D][1], n);
@@ -409,7 +446,7 @@ int split3d_step(Sim *s, double dt)
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
             ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, s->gamma);
-            ks_aux<<<cg, cb, 0, st>>>(f, g, d);
+            ks_aux<<<cg, cb, 0, st>>>(g, d);
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_SWEEP);
@@ -417,19 +454,19 @@ int split3d_step(Sim *s, double dt)
                 constexpr int T = Tile<0>::TA;
                 dim3 b(Tile<0>::TA, Tile<0>::TB);
                 dim3 gr(blocks_for(G.nx - 5, T - 1), blocks_for((long long)G.ny * G.nz, Tile<0>::TB));
-                ks_sweep<0><<<gr, b, 0, st>>>(f, g, make_view(f, g, 0), d, s->odr, s->flux, gam);
+                ks_sweep<0><<<gr, b, 0, st>>>(g, make_view(g, 0), d, s->odr, s->flux, gam);
             }
             {
                 constexpr int T = Tile<1>::TB;
                 dim3 b(Tile<1>::TA, Tile<1>::TB);
                 dim3 gr(blocks_for(G.nx, Tile<1>::TA), blocks_for(G.ny - 5, T - 1), G.nz);
-                ks_sweep<1><<<gr, b, 0, st>>>(f, g, make_view(f, g, 1), d, s->odr, s->flux, gam);
+                ks_sweep<1><<<gr, b, 0, st>>>(g, make_view(g, 1), d, s->odr, s->flux, gam);
             }
             {
                 constexpr int T = Tile<2>::TB;
                 dim3 b(Tile<2>::TA, Tile<2>::TB);
                 dim3 gr(blocks_for(G.nx, Tile<2>::TA), blocks_for(G.nz - 5, T - 1), G.ny);
-                ks_sweep<2><<<gr, b, 0, st>>>(f, g, make_view(f, g, 2), d, s->odr, s->flux, gam);
+                ks_sweep<2><<<gr, b, 0, st>>>(g, make_view(g, 2), d, s->odr, s->flux, gam);
             }
         }
         {
@@ -438,7 +475,9 @@ int split3d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_UPDATE);
-            ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, ra, rb, dt / G.dx, dt / G.dy, dt / G.dz);
+            ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, ra, rb, (float)(dt / G.dx),
+                                         (float)(dt / G.dy), (float)(dt / G.dz), dt / G.dx,
+                                         dt / G.dy, dt / G.dz);
         }
         MLAU_CUDA(cudaGetLastError());
     }
