@@ -143,6 +143,74 @@ int mlau_sim_launches_per_step(mlau_sim *sim);
 int mlau_sim_time_steps(mlau_sim *sim, double dt, int nsteps, double *ms);
 
 /* ---------------------------------------------------------------------- */
+/* 5. Batched 2D engine                                                    */
+/* ---------------------------------------------------------------------- */
+/* Many independent periodic 2D instances (the 2D driver's scheme,
+ * 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c, RK3) in slots of one engine, each with
+ * its own grid size (nx, ny padded), cell sizes, gamma, Riemann solver, CFL
+ * number and end time.  One persistent cooperative kernel per step walks a
+ * per-instance tile table; each instance takes its own CFL dt every step
+ * (clipped to land on its end time) and retires when it gets there.
+ * Precision per engine: MLAU_FP64 (each instance bit-identical to
+ * mhd_fd_ct_2d) or MLAU_FP32_SPLIT.  Instances join and leave between runs
+ * (continuous batching).  No reference counterpart (the reference runs one
+ * problem per process). */
+typedef struct mlau_batch mlau_batch;
+/* Engine with pools of capacity_cells cells and max_inst slots. */
+int mlau_batch_open(mlau_batch **out, int precision, long long capacity_cells, int max_inst,
+                    int off, int odr);
+/* Admit an instance with its initial state (8 host arrays); MLAU_ERR_NOMEM
+ * when no slot or pool space is free (retry after a removal). */
+int mlau_batch_add(mlau_batch *b, int nx, int ny, double dx, double dy, double gamma, int flux,
+                   double cfl, double t_end, const double *const *host8, int *slot);
+int mlau_batch_remove(mlau_batch *b, int slot);
+/* FP32-split engine sized for and filled with ninst instances (zero state;
+ * upload each). */
+int mlau_batch_create(mlau_batch **out, int ninst, const int *nx, const int *ny, int off,
+                      const double *dx, const double *dy, const double *gamma, const int *flux,
+                      const double *cfl, const double *t_end, int odr);
+int mlau_batch_destroy(mlau_batch *b);
+int mlau_batch_upload(mlau_batch *b, int inst, const double *const *host8);
+int mlau_batch_download(mlau_batch *b, int inst, double *const *host8);
+/* dt > 0: fixed time step for that instance instead of its CFL step. */
+int mlau_batch_set_fixed_dt(mlau_batch *b, int inst, double dt);
+/* Tile shape TW x TH (= 256 threads, TW a multiple of 16). */
+int mlau_batch_set_tile(mlau_batch *b, int tw, int th);
+/* Grid of the persistent step kernel: nblocks co-resident blocks (clamped to
+ * what fits, returned), or 0 for all that fit.  Several engines stepping at
+ * once on one GPU each take a share, so that their grids are co-resident
+ * together.  mlau_batch_max_grid: the blocks that fit at the current tile. */
+int mlau_batch_set_grid(mlau_batch *b, int nblocks);
+int mlau_batch_max_grid(mlau_batch *b);
+/* Time `steps` steps per candidate tile shape on the live state and keep the
+ * fastest (the tuning steps advance the simulation). */
+int mlau_batch_autotune(mlau_batch *b, int steps, int *tw, int *th, double *ms);
+/* Advance until every instance has retired or max_steps steps were taken;
+ * steps_per_graph > 0 replays a captured CUDA graph of that many steps. */
+int mlau_batch_run(mlau_batch *b, int max_steps, int steps_per_graph, int *active_left,
+                   double *ms);
+int mlau_batch_info(mlau_batch *b, int inst, double *t, int *steps, int *active);
+/* MLAU_ERR_STATE when the instance retired early because its state held a NaN
+ * or a non-positive density or pressure (the other instances carry on). */
+int mlau_batch_status(mlau_batch *b, int inst);
+long long mlau_batch_cells(mlau_batch *b);
+long long mlau_batch_device_bytes(mlau_batch *b);
+/* Kernel launches issued so far (graph replays counted per step). */
+long long mlau_batch_launches(mlau_batch *b);
+/* 1D engine (FP64): independent 1D problems, each stepped bit-identically to
+ * mhd_fd4c_1d (1D/SERIAL/shock/mhd_fd4c_1d.c:60-271; open boundary
+ * openbc1d_mhd.c:21-175, or periodic).  Each instance's dt is fixed once from
+ * its initial state, dt = cfl*dx/max(1, max|vx|+cf), as the 1D driver's main
+ * does (1D/SERIAL/shock/main.cpp:113-128), unless mlau_batch_set_fixed_dt
+ * gives one; it retires after the step that reaches t_end (the last step is
+ * not clipped).  The other mlau_batch_* calls apply; tiles are 64, 128 or
+ * 256 cells by 1. */
+int mlau_batch1d_open(mlau_batch **out, long long capacity_cells, int max_inst, int off, int odr);
+/* host8: slots 0 ro, 1 mx, 2 my, 3 mz, 4 en, 6 by, 7 bz (slot 5 unused). */
+int mlau_batch1d_add(mlau_batch *b, int nx, double dx, double bx, double gamma, int flux, int nrk,
+                     int bc, double cfl, double t_end, const double *const *host8, int *slot);
+
+/* ---------------------------------------------------------------------- */
 /* 4. Allocation-free 1D step                                              */
 /* ---------------------------------------------------------------------- */
 /* No counterpart in the reference (its drivers malloc scratch on every call).

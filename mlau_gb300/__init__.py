@@ -63,6 +63,27 @@ def _bind(lib):
     lib.mlau_pin_host.argtypes = [vp, C.c_longlong]
     lib.mlau_unpin_host.argtypes = [vp]
     lib.mlau_set_device.argtypes = [i]
+    pi = C.POINTER(C.c_int)
+    lib.mlau_batch_create.argtypes = [C.POINTER(vp), i, pi, pi, i, pd, pd, pd, pi, pd, pd, i]
+    lib.mlau_batch_open.argtypes = [C.POINTER(vp), i, C.c_longlong, i, i, i]
+    lib.mlau_batch_add.argtypes = [vp, i, i, d, d, d, i, d, d, C.POINTER(pd), pi]
+    lib.mlau_batch1d_open.argtypes = [C.POINTER(vp), C.c_longlong, i, i, i]
+    lib.mlau_batch1d_add.argtypes = [vp, i, d, d, d, i, i, i, d, d, C.POINTER(pd), pi]
+    lib.mlau_batch_remove.argtypes = [vp, i]
+    lib.mlau_batch_destroy.argtypes = [vp]
+    lib.mlau_batch_upload.argtypes = [vp, i, C.POINTER(pd)]
+    lib.mlau_batch_download.argtypes = [vp, i, C.POINTER(pd)]
+    lib.mlau_batch_set_fixed_dt.argtypes = [vp, i, d]
+    lib.mlau_batch_set_tile.argtypes = [vp, i, i]
+    lib.mlau_batch_autotune.argtypes = [vp, i, pi, pi, pd]
+    lib.mlau_batch_run.argtypes = [vp, i, i, pi, pd]
+    lib.mlau_batch_info.argtypes = [vp, i, pd, pi, pi]
+    lib.mlau_batch_status.argtypes = [vp, i]
+    lib.mlau_batch_set_grid.argtypes = [vp, i]
+    lib.mlau_batch_max_grid.argtypes = [vp]
+    for f in ("mlau_batch_cells", "mlau_batch_device_bytes", "mlau_batch_launches"):
+        getattr(lib, f).argtypes = [vp]
+        getattr(lib, f).restype = C.c_longlong
     lib.mlau_set_scheme.argtypes = [i, i, i, i]
     lib.mlau_set_bc_1d.argtypes = [i]
     lib.mlau_set_precision.argtypes = [i, i]
@@ -297,3 +318,179 @@ class Sim:
     @property
     def launches_per_step(self) -> int:
         return int(lib().mlau_sim_launches_per_step(self._h))
+
+
+VARS_1D = ("ro", "mx", "my", "mz", "en", None, "by", "bz")
+
+
+class Batch:
+    """Batched engine (include/mlau_gb300.h section 5): slots of periodic 2D
+    instances with their own size, solver, gamma, CFL dt and end time, or (a
+    1D engine) of 1D problems stepped like mhd_fd4c_1d.
+
+    Batch(shapes, ...) fills one slot per shape (FP32-split); Batch.open(...)
+    makes an empty 2D engine that admits instances with add(); Batch.open1d()
+    an empty 1D engine that admits them with add1d()."""
+
+    def __init__(self, shapes=None, dx=None, dy=None, gamma=None, flux=None, cfl=None,
+                 t_end=None, off=4, odr=4, _handle=None, _dim=2):
+        self.shapes = {}
+        self.dim = _dim
+        if _handle is not None:
+            self._h = _handle
+            return
+        n = len(shapes)
+        ai = lambda xs: (C.c_int * n)(*[int(x) for x in xs])
+        ad = lambda xs: (C.c_double * n)(*[float(x) for x in xs])
+        h = C.c_void_p()
+        _check(lib().mlau_batch_create(
+            C.byref(h), n, ai([s[1] for s in shapes]), ai([s[0] for s in shapes]), off, ad(dx),
+            ad(dy), ad(gamma), ai([_flux(f) for f in flux]), ad(cfl), ad(t_end), odr))
+        self._h = h
+        self.shapes = {k: tuple(s) for k, s in enumerate(shapes)}
+
+    @classmethod
+    def open(cls, capacity_cells, max_inst, precision=FP32_SPLIT, off=4, odr=4):
+        h = C.c_void_p()
+        _check(lib().mlau_batch_open(C.byref(h), precision, int(capacity_cells), max_inst, off,
+                                     odr))
+        return cls(_handle=h)
+
+    @classmethod
+    def open1d(cls, capacity_cells, max_inst, off=4, odr=2):
+        h = C.c_void_p()
+        _check(lib().mlau_batch1d_open(C.byref(h), int(capacity_cells), max_inst, off, odr))
+        return cls(_handle=h, _dim=1)
+
+    @property
+    def _vars(self):
+        return VARS_1D if self.dim == 1 else VARS
+
+    def _ptrs(self, state, shape):
+        keep, ptrs = [], (C.POINTER(C.c_double) * 8)()
+        for v, name in enumerate(self._vars):
+            if name is None:
+                continue
+            a = np.ascontiguousarray(state[name], dtype=np.float64)
+            if a.shape != shape:
+                raise MlauError(f"{name}: shape {a.shape} != {shape}")
+            keep.append(a)
+            ptrs[v] = _ptr(a)
+        return keep, ptrs
+
+    def add1d(self, state, dx, bx, gamma, flux="mlau", nrk=3, bc="open", cfl=0.4, t_end=0.1):
+        """Admit a 1D problem (state: ro, mx, my, mz, en, by, bz with ghosts);
+        returns its slot, or None when the engine is full."""
+        shape = np.shape(state["ro"])
+        keep, ptrs = self._ptrs(state, shape)
+        slot = C.c_int()
+        rc = lib().mlau_batch1d_add(self._h, shape[0], dx, bx, gamma, _flux(flux), nrk,
+                                    BC1D[bc] if isinstance(bc, str) else int(bc), cfl, t_end,
+                                    ptrs, C.byref(slot))
+        if rc == -3:
+            return None
+        _check(rc)
+        self.shapes[slot.value] = tuple(shape)
+        return slot.value
+
+    def add(self, state, dx, dy, gamma, flux, cfl, t_end):
+        """Admit an instance; returns its slot, or None when the engine is full."""
+        shape = state["ro"].shape
+        keep = [np.ascontiguousarray(state[v], dtype=np.float64) for v in VARS]
+        ptrs = (C.POINTER(C.c_double) * 8)(*[_ptr(a) for a in keep])
+        slot = C.c_int()
+        rc = lib().mlau_batch_add(self._h, shape[1], shape[0], dx, dy, gamma, _flux(flux), cfl,
+                                  t_end, ptrs, C.byref(slot))
+        if rc == -3:
+            return None
+        _check(rc)
+        self.shapes[slot.value] = tuple(shape)
+        return slot.value
+
+    def remove(self, k):
+        _check(lib().mlau_batch_remove(self._h, k))
+        self.shapes.pop(k, None)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mlau_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, k, state):
+        keep, ptrs = self._ptrs(state, self.shapes[k])
+        _check(lib().mlau_batch_upload(self._h, k, ptrs))
+
+    def download(self, k):
+        out = {v: np.empty(self.shapes[k]) for v in self._vars if v is not None}
+        ptrs = (C.POINTER(C.c_double) * 8)()
+        for v, name in enumerate(self._vars):
+            if name is not None:
+                ptrs[v] = _ptr(out[name])
+        _check(lib().mlau_batch_download(self._h, k, ptrs))
+        return out
+
+    def set_fixed_dt(self, k, dt):
+        _check(lib().mlau_batch_set_fixed_dt(self._h, k, dt))
+
+    def set_tile(self, tw, th):
+        _check(lib().mlau_batch_set_tile(self._h, tw, th))
+
+    def set_grid(self, nblocks):
+        """Blocks of the persistent step kernel (0: all that fit); returns the
+        grid actually used."""
+        rc = lib().mlau_batch_set_grid(self._h, int(nblocks))
+        if rc < 0:
+            _check(rc)
+        return rc
+
+    @property
+    def max_grid(self):
+        return int(lib().mlau_batch_max_grid(self._h))
+
+    def autotune(self, steps=2):
+        tw, th, ms = C.c_int(), C.c_int(), C.c_double()
+        _check(lib().mlau_batch_autotune(self._h, steps, C.byref(tw), C.byref(th), C.byref(ms)))
+        return tw.value, th.value, ms.value
+
+    def run(self, max_steps, steps_per_graph=0):
+        left, ms = C.c_int(), C.c_double()
+        _check(lib().mlau_batch_run(self._h, max_steps, steps_per_graph, C.byref(left),
+                                    C.byref(ms)))
+        return left.value, ms.value
+
+    def info(self, k):
+        t, st, act = C.c_double(), C.c_int(), C.c_int()
+        _check(lib().mlau_batch_info(self._h, k, C.byref(t), C.byref(st), C.byref(act)))
+        return t.value, st.value, bool(act.value)
+
+    def failed(self, k) -> bool:
+        """True when instance k retired on a bad state (NaN, or density or
+        pressure not positive)."""
+        rc = lib().mlau_batch_status(self._h, k)
+        if rc not in (0, -4):
+            _check(rc)
+        return rc == -4
+
+    @property
+    def cells(self):
+        return int(lib().mlau_batch_cells(self._h))
+
+    @property
+    def device_bytes(self):
+        return int(lib().mlau_batch_device_bytes(self._h))
+
+    @property
+    def launches(self):
+        return int(lib().mlau_batch_launches(self._h))

@@ -34,6 +34,10 @@ UNITS = {
     "api.cu": EXACT,
     "peaks.cu": EXACT,
     "noalloc1d.cu": EXACT,
+    "batch2d.cu": EXACT,
+    "batch2d_split.cu": FAST32,
+    "batch2d_plain.cu": EXACT,
+    "batch1d_plain.cu": EXACT,
     "cxx_linkage.cpp": [],
 }
 

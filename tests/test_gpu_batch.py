@@ -1,0 +1,320 @@
+"""Batched 2D engine (FP32-split, one cooperative persistent kernel per step)."""
+import numpy as np
+import pytest
+
+import mlau_gb300 as M
+from mlau_gb300 import ics
+
+pytestmark = pytest.mark.gpu
+
+RHO_L1_TOL = 1e-6
+INT2 = (slice(4, -4),) * 2
+
+
+def l1(a, b):
+    return float(np.abs(a[INT2] - b[INT2]).sum() / np.abs(b[INT2]).sum())
+
+
+def make_cases(sizes, seed=0):
+    rng = np.random.default_rng(seed)
+    cases = []
+    for k, (nx, ny) in enumerate(sizes):
+        st, m = ics.turbulence_2d(n=nx, ny=ny, seed=seed + k, vrms=float(rng.uniform(0.1, 1.2)))
+        cases.append(dict(st=st, m=m, flux=["mlau", "lhlld", "hlld", "roe"][k % 4],
+                          gamma=m["gamma"]))
+    return cases
+
+
+def batch_of(cases, t_end=1.0, cfl=0.4):
+    b = M.Batch([c["st"]["ro"].shape for c in cases], [c["m"]["dx"] for c in cases],
+                [c["m"]["dy"] for c in cases], [c["gamma"] for c in cases],
+                [c["flux"] for c in cases], [cfl] * len(cases), [t_end] * len(cases))
+    for k, c in enumerate(cases):
+        b.upload(k, c["st"])
+    return b
+
+
+def test_alone_equals_in_the_mix():
+    cases = make_cases([(32, 24), (48, 48), (24, 40), (64, 32)], seed=3)
+    with batch_of(cases) as b:
+        for k in range(len(cases)):
+            b.set_fixed_dt(k, 1e-3)
+        b.run(6)
+        mixed = [b.download(k) for k in range(len(cases))]
+    for k, c in enumerate(cases):
+        with batch_of([c]) as b1:
+            b1.set_fixed_dt(0, 1e-3)
+            b1.run(6)
+            alone = b1.download(0)
+        for v in alone:
+            assert np.array_equal(alone[v], mixed[k][v]), (k, v)
+
+
+def test_tile_shape_and_graph_do_not_change_results():
+    cases = make_cases([(40, 32), (32, 56)], seed=5)
+    outs = []
+    for tile, graph in (((32, 8), 0), ((16, 16), 0), ((64, 4), 3), ((128, 2), 2)):
+        with batch_of(cases) as b:
+            b.set_tile(*tile)
+            for k in range(2):
+                b.set_fixed_dt(k, 1e-3)
+            b.run(6, steps_per_graph=graph)
+            outs.append([b.download(k) for k in range(2)])
+    for o in outs[1:]:
+        for k in range(2):
+            for v in o[k]:
+                assert np.array_equal(o[k][v], outs[0][k][v])
+
+
+def test_split_vs_fp64_plain():
+    st, m = ics.turbulence_2d(n=64, seed=2, vrms=0.5)
+    dt = 0.4 * m["dx"] / m["vfast"]
+    with M.Sim(2, st["ro"].shape, dx=m["dx"], dy=m["dy"], odr=4, flux="lhlld") as s:
+        s.upload(st)
+        s.step(dt, 40)
+        ref = s.download()
+    with M.Batch([st["ro"].shape], [m["dx"]], [m["dy"]], [m["gamma"]], ["lhlld"], [0.4],
+                 [1.0]) as b:
+        b.upload(0, st)
+        b.set_fixed_dt(0, dt)
+        b.run(40)
+        got = b.download(0)
+    assert l1(got["ro"], ref["ro"]) <= RHO_L1_TOL
+    assert l1(got["en"], ref["en"]) <= 1e-6
+    assert not got["mz"].any() and not got["bz"].any()
+    assert ics.div_b_2d(got, m["dx"], m["dy"]) <= 1e-12
+
+
+def test_cfl_dt_and_retirement():
+    cases = make_cases([(32, 32), (48, 24), (24, 24)], seed=9)
+    t_ends = [0.01, 0.02, 0.015]
+    b = M.Batch([c["st"]["ro"].shape for c in cases], [c["m"]["dx"] for c in cases],
+                [c["m"]["dy"] for c in cases], [c["gamma"] for c in cases],
+                [c["flux"] for c in cases], [0.4] * 3, t_ends)
+    with b:
+        for k, c in enumerate(cases):
+            b.upload(k, c["st"])
+        left, ms = b.run(10000, steps_per_graph=8)
+        assert left == 0
+        for k in range(3):
+            t, steps, active = b.info(k)
+            assert not active and abs(t - t_ends[k]) <= 1e-12 * t_ends[k] and steps >= 2
+            assert np.isfinite(b.download(k)["en"]).all()
+
+
+def test_fp64_engine_equals_single_instance_with_cfl():
+    """FP64 engine: every instance, with its own per-step CFL dt, advances bit
+    for bit like the single-instance plain 2D path."""
+    cases = make_cases([(40, 32), (24, 48), (32, 32)], seed=11)
+    refs = []
+    for c in cases:
+        m = c["m"]
+        with M.Sim(2, c["st"]["ro"].shape, dx=m["dx"], dy=m["dy"], gamma=c["gamma"], odr=4,
+                   flux=c["flux"]) as s:
+            s.upload(c["st"])
+            for _ in range(5):
+                dt, _ = s.cfl(0.4, min(m["dx"], m["dy"]), 0.0, 0.0)
+                s.step(dt, 1)
+            refs.append(s.download())
+    cells = sum(c["st"]["ro"].size for c in cases)
+    b = M.Batch.open(cells, 4, precision=M.FP64)
+    with b:
+        slots = [b.add(c["st"], c["m"]["dx"], c["m"]["dy"], c["gamma"], c["flux"], 0.4, 10.0)
+                 for c in cases]
+        b.run(5)
+        for k, sl in enumerate(slots):
+            got = b.download(sl)
+            for v in got:
+                assert np.array_equal(got[v], refs[k][v]), (k, v)
+
+
+def test_continuous_batching_join_and_leave():
+    """Instances join and leave between runs; each result equals the same
+    instance run alone (FP64 engine: bit for bit)."""
+    cases = make_cases([(32, 32), (48, 24), (24, 40)], seed=13)
+    for c in cases:
+        c["dt"] = 2e-3
+
+    def alone(c, steps):
+        with M.Batch.open(c["st"]["ro"].size, 1, precision=M.FP64) as b1:
+            s = b1.add(c["st"], c["m"]["dx"], c["m"]["dy"], c["gamma"], c["flux"], 0.4, 10.0)
+            b1.set_fixed_dt(s, c["dt"])
+            b1.run(steps)
+            return b1.download(s)
+
+    cap = cases[0]["st"]["ro"].size + cases[1]["st"]["ro"].size + 64
+    with M.Batch.open(cap, 2, precision=M.FP64) as b:
+        s0 = b.add(cases[0]["st"], cases[0]["m"]["dx"], cases[0]["m"]["dy"], cases[0]["gamma"],
+                   cases[0]["flux"], 0.4, 10.0)
+        b.set_fixed_dt(s0, 2e-3)
+        b.run(3)
+        s1 = b.add(cases[1]["st"], cases[1]["m"]["dx"], cases[1]["m"]["dy"], cases[1]["gamma"],
+                   cases[1]["flux"], 0.4, 10.0)
+        b.set_fixed_dt(s1, 2e-3)
+        assert b.add(cases[2]["st"], cases[2]["m"]["dx"], cases[2]["m"]["dy"],
+                     cases[2]["gamma"], cases[2]["flux"], 0.4, 10.0) is None  # full
+        b.run(4, steps_per_graph=2)
+        r0 = b.download(s0)
+        b.remove(s0)
+        s2 = b.add(cases[2]["st"], cases[2]["m"]["dx"], cases[2]["m"]["dy"], cases[2]["gamma"],
+                   cases[2]["flux"], 0.4, 10.0)
+        b.set_fixed_dt(s2, 2e-3)
+        b.run(2)
+        r1, r2 = b.download(s1), b.download(s2)
+    for got, c, n in ((r0, cases[0], 7), (r1, cases[1], 6), (r2, cases[2], 2)):
+        want = alone(c, n)
+        for v in want:
+            assert np.array_equal(got[v], want[v]), (n, v)
+
+
+# --- 1D engine ---------------------------------------------------------------
+V1 = ("ro", "mx", "my", "mz", "en", "by", "bz")
+
+
+def cases_1d(ns, seed=0):
+    out = []
+    for k, n in enumerate(ns):
+        st, m = ics.riemann_1d(n=n, seed=seed + k)
+        out.append(dict(st=st, m=m, flux=["mlau", "lhlld", "hlld", "roe"][k % 4],
+                        nrk=[3, 2, 1, 3][k % 4], bc=["open", "periodic"][(k // 2) % 2]))
+    return out
+
+
+def oracle_solution(port, c, t_end, cfl=0.4, odr=2):
+    """The reference's 1D driver loop on the CPU: dt fixed from the initial
+    state, `t += dt` until t reaches t_end."""
+    st, m = ics.copy_state(c["st"]), c["m"]
+    dt = port.dt1d(st, m["bx"], m["gamma"], cfl, m["dx"])
+    t, n = 0.0, 0
+    while True:
+        port.step1d(st, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=c["flux"],
+                     nrk=c["nrk"], bc=c["bc"])
+        t += dt
+        n += 1
+        if t >= t_end:
+            return st, n, t
+
+
+def batch1d_of(cases, t_end, odr=2):
+    b = M.Batch.open1d(sum(c["st"]["ro"].size for c in cases) + 64, len(cases) + 2, odr=odr)
+    for c in cases:
+        m = c["m"]
+        c["slot"] = b.add1d(c["st"], m["dx"], m["bx"], m["gamma"], c["flux"], c["nrk"],
+                            c["bc"], 0.4, t_end)
+    return b
+
+
+def test_batch1d_each_instance_equals_the_oracle(port):
+    cases = cases_1d([64, 100, 48, 80, 72, 56, 90, 40], seed=11)
+    with batch1d_of(cases, t_end=0.02) as b:
+        left, _ = b.run(100000)
+        assert left == 0
+        for c in cases:
+            ref, n, t = oracle_solution(port, c, 0.02)
+            got = b.download(c["slot"])
+            tb, nb, act = b.info(c["slot"])
+            assert (nb, act) == (n, False) and tb == t
+            for v in V1:
+                assert np.array_equal(got[v], ref[v]), (c["flux"], c["nrk"], c["bc"], v)
+
+
+def test_batch1d_alone_equals_in_the_mix_and_graphs():
+    cases = cases_1d([128, 300, 64, 257, 512, 96], seed=21)
+    outs = []
+    for tile, graph in (((256, 1), 0), ((128, 1), 4), ((64, 1), 7)):
+        with batch1d_of(cases, t_end=0.03) as b:
+            b.set_tile(*tile)
+            left, _ = b.run(100000, steps_per_graph=graph)
+            assert left == 0
+            outs.append([b.download(c["slot"]) for c in cases])
+    for o in outs[1:]:
+        for k in range(len(cases)):
+            for v in V1:
+                assert np.array_equal(o[k][v], outs[0][k][v])
+    for k, c in enumerate(cases):
+        with batch1d_of([c], t_end=0.03) as b1:
+            b1.run(100000)
+            alone = b1.download(c["slot"])
+        for v in V1:
+            assert np.array_equal(alone[v], outs[0][k][v]), (k, v)
+
+
+def test_batch1d_join_leave_and_dropin_equality(port):
+    """Continuous batching in the 1D engine: instances admitted while others
+    run give the drop-in driver's result."""
+    cases = cases_1d([80, 120, 60, 100], seed=31)
+    for c in cases:
+        c["flux"], c["nrk"], c["bc"] = "mlau", 2, "open"  # the drop-in's 1D default scheme
+    b = M.Batch.open1d(400, 3, odr=1)
+    try:
+        m0 = cases[0]["m"]
+        s0 = b.add1d(cases[0]["st"], m0["dx"], m0["bx"], m0["gamma"], "mlau", 2, "open", 0.4, 0.05)
+        s1 = b.add1d(cases[1]["st"], cases[1]["m"]["dx"], cases[1]["m"]["bx"],
+                     cases[1]["m"]["gamma"], "mlau", 2, "open", 0.4, 0.05)
+        b.run(20)
+        s2 = b.add1d(cases[2]["st"], cases[2]["m"]["dx"], cases[2]["m"]["bx"],
+                     cases[2]["m"]["gamma"], "mlau", 2, "open", 0.4, 0.05)
+        assert b.add1d(cases[3]["st"], cases[3]["m"]["dx"], cases[3]["m"]["bx"],
+                       cases[3]["m"]["gamma"], "mlau", 2, "open", 0.4, 0.05) is None
+        b.run(100000)
+        for c, s in zip(cases[:3], (s0, s1, s2)):
+            m = c["m"]
+            st = ics.copy_state(c["st"])
+            dt = port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
+            M.set_scheme(1, 1, "mlau", 2)
+            M.set_bc_1d("open")
+            _, n, _ = b.info(s)
+            for _ in range(n):
+                M.mhd_fd4c_1d(*[st[v] for v in V1], m["bx"], dt, m["dx"], st["ro"].shape[0], 4,
+                              m["gamma"])
+            got = b.download(s)
+            for v in V1:
+                assert np.array_equal(got[v], st[v]), v
+    finally:
+        b.close()
+        M.release_dropin()
+
+
+@pytest.mark.parametrize("precision", [M.FP64, M.FP32_SPLIT])
+def test_bad_state_retires_only_that_instance(precision):
+    """A request whose initial state holds negative pressure (fault injected on
+    the host) retires with an error status after at most one step; the other
+    instances finish exactly as they do alone."""
+    cases = make_cases([(40, 32), (32, 40), (48, 24)], seed=41)
+    bad = ics.copy_state(cases[1]["st"])
+    bad["en"][10:14, 10:14] = 0.0  # p < 0 there
+    cases[1]["st"] = bad
+    t_end = 0.01
+
+    def run(cs):
+        b = M.Batch.open(sum(c["st"]["ro"].size for c in cs), len(cs), precision=precision)
+        slots = [b.add(c["st"], c["m"]["dx"], c["m"]["dy"], c["gamma"], c["flux"], 0.4, t_end)
+                 for c in cs]
+        left, _ = b.run(10000)
+        assert left == 0
+        return b, slots
+
+    b, slots = run(cases)
+    with b:
+        assert b.failed(slots[1]) and not b.failed(slots[0]) and not b.failed(slots[2])
+        t1, n1, act1 = b.info(slots[1])
+        assert n1 <= 1 and not act1
+        for k in (0, 2):
+            t, n, act = b.info(slots[k])
+            assert not act and t == pytest.approx(t_end, rel=1e-12) and n > 1
+            mixed = b.download(slots[k])
+            b1, s1 = run([cases[k]])
+            with b1:
+                alone = b1.download(s1[0])
+            for v in alone:
+                assert np.array_equal(alone[v], mixed[v]), (k, v)
+
+
+def test_batch1d_bad_state_retires():
+    cases = cases_1d([64, 64], seed=51)
+    cases[0]["st"]["ro"][20] = -1.0
+    with batch1d_of(cases, t_end=0.02) as b:
+        left, _ = b.run(100000)
+        assert left == 0
+        assert b.failed(cases[0]["slot"]) and not b.failed(cases[1]["slot"])
+        assert b.info(cases[0]["slot"])[1] == 1
