@@ -207,7 +207,7 @@ int mlau_sim_download(mlau_sim *s, double *const *h)
                                   cudaMemcpyDeviceToHost, s->stream));
     }
     MLAU_CUDA(cudaStreamSynchronize(s->stream));
-    return MLAU_OK;
+    return s->sp ? split3d_check(s) : MLAU_OK;
 }
 
 int mlau_sim_set_bx_1d(mlau_sim *s, double bx)
@@ -262,7 +262,7 @@ int mlau_sim_sync(mlau_sim *s)
 {
     if (!s) { set_error("null simulation"); return MLAU_ERR_ARG; }
     MLAU_CUDA(cudaStreamSynchronize(s->stream));
-    return MLAU_OK;
+    return s->sp ? split3d_check(s) : MLAU_OK;
 }
 
 void *mlau_sim_stream(mlau_sim *s) { return s ? (void *)s->stream : nullptr; }

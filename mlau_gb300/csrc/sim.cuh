@@ -53,6 +53,7 @@ int plain1d_step(Sim *s, double dt);
 int split3d_alloc(Sim *s);
 int split3d_step(Sim *s, double dt);
 void split3d_free(Sim *s);
+int split3d_check(Sim *s);
 int cfl_compute(Sim *s, double *vmax_out);
 int launches_per_step(const Sim *s);
 

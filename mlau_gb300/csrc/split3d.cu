@@ -22,15 +22,41 @@
 //
 // Kernels per RK stage: prep (FP64 primitive recovery -> float pairs), aux
 // (FP32 CT weights and shock sensors), one fused reconstruction + flux kernel
-// per direction (shared-memory tile: each thread reconstructs one cell, then
-// each face thread solves one Riemann problem), emf (FP32), update (FP64 RK
-// combine + CT curl + periodic ghost images).
+// per direction, emf (FP32), update (FP64 RK combine + CT curl + periodic
+// ghost images).
+//
+// The fused sweep is a persistent kernel over tiles.  Each tile's inputs (the
+// 5-point stencils of eight float-pair arrays and four float arrays, halo
+// included) are staged in shared memory by the tensor memory accelerator
+// (cp.async.bulk.tensor), double-buffered: while a block computes one tile,
+// the copy of its next tile is in flight.  Then each thread reconstructs one
+// cell into shared memory and, after a block barrier, each face thread solves
+// one Riemann problem.
+//
+// Every FP32 scratch array uses a row pitch px = nx rounded up to a multiple
+// of 4 elements, so that its rows start on 16-byte boundaries as the tensor
+// maps require; the FP64 state keeps the reference layout.
 #include "sim.cuh"
 #include "point.cuh"
+#include "tma.cuh"
+
+#include <algorithm>
 
 namespace mlau {
 
-struct SplitFields {
+// Arrays staged for a sweep, in the sweep's rotated order: density, normal /
+// tangential / third velocity, the two tangential cell B components,
+// pressure, the normal cell B (float pairs); then Mach^2, the face B normal
+// to the sweep, and the two tangential shock sensors (floats).
+enum { SQ_RO, SQ_VN, SQ_VT, SQ_VU, SQ_BT, SQ_BU, SQ_PR, SQ_BN, NQ };
+enum { SF_M2, SF_BF, SF_DVT, SF_DVU, NF };
+
+struct SweepMaps {
+    CUtensorMap q[NQ];
+    CUtensorMap f[NF];
+};
+
+struct SplitPtrs {
     float2 *q[8];    // ro, vx, vy, vz, cx, cy, cz, pr as (hi, lo) pairs
     float *bf[3];    // face-centred bx, by, bz rounded to FP32
     float *F[3][7];
@@ -41,13 +67,30 @@ struct SplitFields {
     float *dv[3];
 };
 
+struct SplitFields {
+    SplitPtrs p{};
+    long long px = 0;       // row pitch of the FP32 scratch (elements)
+    SweepMaps maps[3];      // per sweep direction
+    int ntile[3][2] = {};   // tiles along the first two tile axes, per sweep
+    int ntiles[3] = {};
+    int nblocks[3] = {};    // persistent grid per sweep
+    int *d_err = nullptr;   // set when a bounded wait gave up
+};
+
 namespace {
 
 struct Dims {
     int nx, ny, nz, ox, oy, oz;
+    long long px;  // row pitch of the FP32 scratch
+    // FP64 state (reference layout)
     __device__ __forceinline__ long long at(int i, int j, int k) const
     {
         return (long long)nx * ((long long)ny * k + j) + i;
+    }
+    // FP32 scratch (pitched rows)
+    __device__ __forceinline__ long long ap(int i, int j, int k) const
+    {
+        return px * ((long long)ny * k + j) + i;
     }
 };
 
@@ -59,7 +102,7 @@ __device__ __forceinline__ float2 split2(double x)
 }
 
 __global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitFields g, Dims d, int odr, double gamma)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, double gamma)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= d.nx) return;
@@ -69,7 +112,7 @@ ks_prim(PlainFields f, SplitFields g, Dims d, int odr, double gamma)
     const double cx = face2cen(odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
     const double cy = face2cen(odr, by[w - sy], by[w], by[w + sy], by[w + 2 * sy]);
     const double cz = face2cen(odr, bz[w - sz], bz[w], bz[w + sz], bz[w + 2 * sz]);
-    const long long s = d.at(i, j, k);
+    const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
     const double ro = f.s[0][s];
     // Velocities and the kinetic energy in FP32: rho v^2/2 enters the pressure
     // as an additive term, so its FP32 rounding (1e-7 of itself) stays below
@@ -81,18 +124,18 @@ ks_prim(PlainFields f, SplitFields g, Dims d, int odr, double gamma)
     const float v2 = vx * vx + vy * vy + vz * vz;
     const double b2 = cx * cx + cy * cy + cz * cz;
     const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * ((double)(rof * v2) + b2));
-    g.q[0][s] = split2(ro);
-    g.q[1][s] = make_float2(vx, 0.f);
-    g.q[2][s] = make_float2(vy, 0.f);
-    g.q[3][s] = make_float2(vz, 0.f);
-    g.q[4][s] = split2(cx);
-    g.q[5][s] = split2(cy);
-    g.q[6][s] = split2(cz);
-    g.q[7][s] = split2(pr);
-    g.bf[0][s] = (float)bx[s];
-    g.bf[1][s] = (float)by[s];
-    g.bf[2][s] = (float)bz[s];
-    g.m2[s] = v2 / ((float)gamma * (float)pr * irof);
+    g.q[0][sp] = split2(ro);
+    g.q[1][sp] = make_float2(vx, 0.f);
+    g.q[2][sp] = make_float2(vy, 0.f);
+    g.q[3][sp] = make_float2(vz, 0.f);
+    g.q[4][sp] = split2(cx);
+    g.q[5][sp] = split2(cy);
+    g.q[6][sp] = split2(cz);
+    g.q[7][sp] = split2(pr);
+    g.bf[0][sp] = (float)bx[s];
+    g.bf[1][sp] = (float)by[s];
+    g.bf[2][sp] = (float)bz[s];
+    g.m2[sp] = v2 / ((float)gamma * (float)pr * irof);
 }
 
 // --- CT weights and shock sensors (FP32) ----------------------------------
@@ -120,160 +163,248 @@ __device__ __forceinline__ float ct_w(const float2 *va, const float2 *vb, const 
     return (a + 0.5f * eps) / (a + c + eps);
 }
 
-__global__ void __launch_bounds__(256) ks_aux(SplitFields g, Dims d)
+__global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= d.nx) return;
-    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
-    const long long s = d.at(i, j, k);
+    const long long sy = d.px, sz = d.px * d.ny;
+    const long long s = d.ap(i, j, k);
     const float2 *ro = g.q[0], *vx = g.q[1], *vy = g.q[2], *vz = g.q[3];
     g.ct[0][s] = (i >= 1 && j >= 1) ? ct_w(vx, vy, ro, g.bf[0], g.bf[1], s, sy, 1, sy, 1) : 0.5f;
     g.ct[1][s] = (j >= 1 && k >= 1) ? ct_w(vy, vz, ro, g.bf[1], g.bf[2], s, sz, sy, sz, sy) : 0.5f;
     g.ct[2][s] = (k >= 1 && i >= 1) ? ct_w(vz, vx, ro, g.bf[2], g.bf[0], s, sz, 1, 1, sz) : 0.5f;
-    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
+    const long long w = d.ap(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
     g.dv[0][s] = fminf(qd(vx, w + 1, w), qd(vx, w, w - 1));
     g.dv[1][s] = fminf(qd(vy, w + sy, w), qd(vy, w, w - sy));
     g.dv[2][s] = fminf(qd(vz, w + sz, w), qd(vz, w, w - sz));
 }
 
 // --- fused reconstruction + Riemann flux along axis D ----------------------
-// Rotated views: normal/tangential velocity, cell B (normal, t, u), face B.
-struct View {
-    const float2 *vn, *vt, *vu, *cn, *ct, *cu;
-    const float *bface, *dvt, *dvu;
+// Tile geometry.  Threads: TA along x times TB along the second axis.  For D=0
+// the sweep runs along x (TA = T cells per tile, TB rows of one z-plane); for
+// D=1,2 along y or z (TB = T cells per tile, TA columns of x).  A tile of T
+// cells yields T-1 faces; consecutive tiles along the sweep overlap by one
+// cell.  The staged box (BX, BY, BZ elements, x fastest) covers the tile's
+// stencils: 2 cells of halo on each side along the sweep; for D=0 its x
+// origin is rounded down to a multiple of 4 elements (16-byte TMA rule), so
+// the box is 40 wide and the tile starts at offset x0 - xs in it.
+template <int D> struct SG;
+template <> struct SG<0> {
+    static constexpr int TA = 32, TB = 4, T = 32;
+    static constexpr int BX = 40, BY = 4, BZ = 1;
+};
+template <> struct SG<1> {
+    static constexpr int TA = 16, TB = 16, T = 16;
+    static constexpr int BX = 16, BY = 20, BZ = 1;
+};
+template <> struct SG<2> {
+    static constexpr int TA = 16, TB = 16, T = 16;
+    static constexpr int BX = 16, BY = 1, BZ = 20;
+};
+template <int D> __host__ __device__ constexpr int box_elems() { return SG<D>::BX * SG<D>::BY * SG<D>::BZ; }
+template <int D> __host__ __device__ constexpr unsigned stage_bytes()
+{
+    return (unsigned)(box_elems<D>() * (NQ * sizeof(float2) + NF * sizeof(float)));
+}
+template <int D> constexpr size_t sweep_dyn_smem() { return 2 * stage_bytes<D>() + 128; }
+
+struct TileAt {
+    int x, y, z;   // box origin (elements)
+    int i0, j0, k0;  // cell of thread (0, 0)
+    int off;       // D=0: x offset of the tile inside the box
 };
 
-// Tile: TA threads along the fast (x) axis x TB along the second axis.  For
-// D=0 the sweep runs along x (TA cells per tile, TB rows); for D=1,2 it runs
-// along the second axis (TB cells per tile, TA columns of x).  A tile of T
-// cells yields T-1 faces; consecutive tiles overlap by one cell.
-template <int D> struct Tile;
-template <> struct Tile<0> { static constexpr int TA = 32, TB = 4; };
-template <> struct Tile<1> { static constexpr int TA = 16, TB = 16; };
-template <> struct Tile<2> { static constexpr int TA = 16, TB = 16; };
+// Tile t of a sweep: n0 tiles along the first tile axis, n1 along the second.
+template <int D> __device__ __forceinline__ TileAt tile_at(int t, int n0, int n1)
+{
+    constexpr int T = SG<D>::T;
+    const int t0 = t % n0, r = t / n0, t1 = r % n1, t2 = r / n1;
+    TileAt a;
+    if (D == 0) {
+        const int x0 = 2 + (T - 1) * t0;
+        a.x = (x0 - 2) & ~3;
+        a.y = SG<0>::TB * t1;
+        a.z = t2;
+        a.i0 = x0; a.j0 = a.y; a.k0 = t2;
+        a.off = x0 - a.x;
+    } else if (D == 1) {
+        const int y0 = 2 + (T - 1) * t1;
+        a.x = SG<1>::TA * t0;
+        a.y = y0 - 2;
+        a.z = t2;
+        a.i0 = a.x; a.j0 = y0; a.k0 = t2;
+        a.off = 0;
+    } else {
+        const int z0 = 2 + (T - 1) * t1;
+        a.x = SG<2>::TA * t0;
+        a.y = t2;
+        a.z = z0 - 2;
+        a.i0 = a.x; a.j0 = t2; a.k0 = z0;
+        a.off = 0;
+    }
+    return a;
+}
 
-// Per-cell results in shared memory, stored variable-major ([var][TB][TA]) so
-// that the lanes of a warp touch consecutive words (no bank conflicts):
-//   sl - perturbation at the cell's right face (left state of face c+1) + 2 central parts
-//   sr - at its left face (right state of face c) + 2 central parts
-//   sb - the cell-centre state (ro, vn, vt, vu, bt, bu, pr) as (hi, lo)
+// Box element of stencil point m (0..4, centre 2) of thread (ta, tb).
+template <int D> __device__ __forceinline__ int bidx(const TileAt &a, int ta, int tb, int m)
+{
+    if (D == 0) return tb * SG<0>::BX + a.off + ta + (m - 2);
+    return (tb + m) * SG<D>::TA + ta;
+}
 
 template <int D>
-__global__ void __launch_bounds__(Tile<D>::TA *Tile<D>::TB)
-ks_sweep(SplitFields g, View v, Dims d, int odr, int which, float gamma)
+__device__ __forceinline__ void issue_tile(const SweepMaps &M, unsigned char *st, const TileAt &a,
+                                           uint64_t *bar)
 {
-    constexpr int TA = Tile<D>::TA, TB = Tile<D>::TB;
-    constexpr int T = (D == 0) ? TA : TB;  // cells per tile along the sweep
+    constexpr int NB = box_elems<D>();
+    mbar_expect_tx(bar, stage_bytes<D>());
+#pragma unroll
+    for (int n = 0; n < NQ; n++) tma_load_3d(st + n * NB * sizeof(float2), &M.q[n], a.x, a.y, a.z, bar);
+#pragma unroll
+    for (int n = 0; n < NF; n++)
+        tma_load_3d(st + NQ * NB * sizeof(float2) + n * NB * sizeof(float), &M.f[n], a.x, a.y, a.z,
+                    bar);
+}
+
+template <int D>
+__global__ void __launch_bounds__(SG<D>::TA *SG<D>::TB)
+ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr, int which, float gamma,
+         int n0, int n1, int ntiles, int *err)
+{
+    constexpr int TA = SG<D>::TA, TB = SG<D>::TB, NB = box_elems<D>();
+    constexpr unsigned STAGE = stage_bytes<D>();
+    extern __shared__ unsigned char dyn_smem[];
+    unsigned char *stages =
+        (unsigned char *)(((uintptr_t)dyn_smem + 127) & ~(uintptr_t)127);
+    // per-cell results: sl/sr - perturbation at the cell's right / left face
+    // + 2 central parts; sb - the cell-centre state as (hi, lo)
     __shared__ float sl[9][TB][TA], sr[9][TB][TA];
     __shared__ float2 sb[7][TB][TA];
-    const int ta = threadIdx.x, tb = threadIdx.y;
+    __shared__ uint64_t bar[2];
+    const int ta = threadIdx.x, tb = threadIdx.y, tid = tb * TA + ta;
     const int p = (D == 0) ? ta : tb;  // position along the sweep inside the tile
-    int i, j, k, len;
-    long long st;
-    if (D == 0) {
-        len = d.nx;
-        st = 1;
-        i = 2 + blockIdx.x * (T - 1) + ta;
-        const long long row = (long long)blockIdx.y * TB + tb;
-        j = (int)(row % d.ny);
-        k = (int)(row / d.ny);
-        if (row >= (long long)d.ny * d.nz) k = d.nz;  // out of range
-    } else if (D == 1) {
-        len = d.ny;
-        st = d.nx;
-        i = blockIdx.x * TA + ta;
-        j = 2 + blockIdx.y * (T - 1) + tb;
-        k = blockIdx.z;
-    } else {
-        len = d.nz;
-        st = (long long)d.nx * d.ny;
-        i = blockIdx.x * TA + ta;
-        k = 2 + blockIdx.y * (T - 1) + tb;
-        j = blockIdx.z;
-    }
-    const int a = (D == 0) ? i : (D == 1 ? j : k);  // sweep coordinate
-    const bool in_box = i < d.nx && j < d.ny && k < d.nz;
-    const bool do_rec = in_box && a >= 2 && a < len - 2;
-    const long long c = in_box ? d.at(i, j, k) : 0;
+    const int len = (D == 0) ? d.nx : (D == 1 ? d.ny : d.nz);
 
-    if (do_rec) {
-        const float2 *src[7] = {g.q[0], v.vn, v.vt, v.vu, v.ct, v.cu, g.q[7]};
-        float dq[7][5], qc[7];
-        unsigned zero = 0;
-#pragma unroll
-        for (int n = 0; n < 7; n++) {
-            float2 h[5];
-#pragma unroll
-            for (int m = 0; m < 5; m++) h[m] = src[n][c + st * (m - 2)];
-            qc[n] = h[2].x + h[2].y;
-            bool z = true;
-#pragma unroll
-            for (int m = 0; m < 5; m++) {
-                dq[n][m] = (h[m].x - h[2].x) + (h[m].y - h[2].y);
-                z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
-            }
-            if (z) zero |= 1u << n;
-            sb[n][tb][ta] = h[2];
-        }
-        float ul[7], ur[7];
-        const float bnc = qf(v.cn, c);
-        const float mm = fmaxf(g.m2[c - st], fmaxf(g.m2[c], g.m2[c + st]));
-        if (mm >= 1.0f) reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
-        else reconst_alfven_core(odr, dq, qc, bnc, gamma, ul, ur);
-#pragma unroll
-        for (int n = 1; n <= 5; n++)
-            if (zero & (1u << n)) { ul[n] = 0.f; ur[n] = 0.f; }
-#pragma unroll
-        for (int n = 0; n < 7; n++) { sl[n][tb][ta] = ul[n]; sr[n][tb][ta] = ur[n]; }
-        // central parts of the two tangential B fluxes: lin(bt vn) - bn_face lin(vt)
-        const float bl = v.bface[c + st], br = v.bface[c];
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            const int kb = 4 + t, kv = 2 + t;
-            const float a0 = (qc[kb]) * (qc[1]);
-            float da[5];
-#pragma unroll
-            for (int m = 0; m < 5; m++)
-                da[m] = (qc[kb] + dq[kb][m]) * (qc[1] + dq[1][m]) - a0;
-            const float al = a0 + lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
-            const float ar = a0 + lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
-            const float vl = qc[kv] + lin_l(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
-            const float vr = qc[kv] + lin_r(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
-            sl[7 + t][tb][ta] = al - bl * vl;
-            sr[7 + t][tb][ta] = ar - br * vr;
-        }
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_async_shared();
     }
     __syncthreads();
+    if (tid == 0 && (int)blockIdx.x < ntiles)
+        issue_tile<D>(M, stages, tile_at<D>(blockIdx.x, n0, n1), &bar[0]);
 
-    if (!in_box || p == 0 || a < 3 || a >= len - 2) return;
-    const int tbl = (D == 0) ? tb : tb - 1, tal = (D == 0) ? ta - 1 : ta;
-    float L[7], Rr[7];
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+        const int b = it & 1;
+        const int tn = t + gridDim.x;
+        if (tid == 0 && tn < ntiles) {
+            // the other buffer was released by the barrier that ended the
+            // previous iteration
+            fence_async_shared();
+            issue_tile<D>(M, stages + (b ^ 1) * STAGE, tile_at<D>(tn, n0, n1), &bar[b ^ 1]);
+        }
+        const bool ok = mbar_wait(&bar[b], (it >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                if (tn < ntiles) mbar_wait(&bar[b ^ 1], ((it + 1) >> 1) & 1);
+            }
+            return;
+        }
+        const float2 *Q = (const float2 *)(stages + b * STAGE);
+        const float *Fs = (const float *)(stages + b * STAGE + NQ * NB * sizeof(float2));
+        const TileAt a = tile_at<D>(t, n0, n1);
+        const int i = a.i0 + ta, j = a.j0 + ((D == 2) ? 0 : tb), k = a.k0 + ((D == 2) ? tb : 0);
+        const int ac = (D == 0) ? i : (D == 1 ? j : k);  // sweep coordinate
+        const bool in_box = i < d.nx && j < d.ny && k < d.nz;
+        const bool do_rec = in_box && ac >= 2 && ac < len - 2;
+        auto QI = [&](int n, int m) { return Q[n * NB + bidx<D>(a, ta, tb, m)]; };
+        auto FI = [&](int n, int m) { return Fs[n * NB + bidx<D>(a, ta, tb, m)]; };
+
+        if (do_rec) {
+            float dq[7][5], qc[7];
+            unsigned zero = 0;
 #pragma unroll
-    for (int n = 0; n < 7; n++) {
-        L[n] = (sb[n][tbl][tal].x + sb[n][tbl][tal].y) + sl[n][tbl][tal];
-        Rr[n] = (sb[n][tb][ta].x + sb[n][tb][ta].y) + sr[n][tb][ta];
+            for (int n = 0; n < 7; n++) {
+                float2 h[5];
+#pragma unroll
+                for (int m = 0; m < 5; m++) h[m] = QI(n, m);
+                qc[n] = h[2].x + h[2].y;
+                bool z = true;
+#pragma unroll
+                for (int m = 0; m < 5; m++) {
+                    dq[n][m] = (h[m].x - h[2].x) + (h[m].y - h[2].y);
+                    z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
+                }
+                if (z) zero |= 1u << n;
+                sb[n][tb][ta] = h[2];
+            }
+            float ul[7], ur[7];
+            const float2 bn2 = QI(SQ_BN, 2);
+            const float bnc = bn2.x + bn2.y;
+            const float mm = fmaxf(FI(SF_M2, 1), fmaxf(FI(SF_M2, 2), FI(SF_M2, 3)));
+            if (mm >= 1.0f) reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
+            else reconst_alfven_core(odr, dq, qc, bnc, gamma, ul, ur);
+#pragma unroll
+            for (int n = 1; n <= 5; n++)
+                if (zero & (1u << n)) { ul[n] = 0.f; ur[n] = 0.f; }
+#pragma unroll
+            for (int n = 0; n < 7; n++) { sl[n][tb][ta] = ul[n]; sr[n][tb][ta] = ur[n]; }
+            // central parts of the two tangential B fluxes: lin(bt vn) - bn_face lin(vt)
+            const float bl = FI(SF_BF, 3), br = FI(SF_BF, 2);
+#pragma unroll
+            for (int tt = 0; tt < 2; tt++) {
+                const int kb = 4 + tt, kv = 2 + tt;
+                const float a0 = (qc[kb]) * (qc[1]);
+                float da[5];
+#pragma unroll
+                for (int m = 0; m < 5; m++)
+                    da[m] = (qc[kb] + dq[kb][m]) * (qc[1] + dq[1][m]) - a0;
+                const float al = a0 + lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
+                const float ar = a0 + lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
+                const float vl = qc[kv] + lin_l(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
+                const float vr = qc[kv] + lin_r(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
+                sl[7 + tt][tb][ta] = al - bl * vl;
+                sr[7 + tt][tb][ta] = ar - br * vr;
+            }
+        }
+        __syncthreads();
+
+        if (in_box && p >= 1 && ac >= 3 && ac < len - 2) {
+            const int tbl = (D == 0) ? tb : tb - 1, tal = (D == 0) ? ta - 1 : ta;
+            float L[7], Rr[7];
+#pragma unroll
+            for (int n = 0; n < 7; n++) {
+                L[n] = (sb[n][tbl][tal].x + sb[n][tbl][tal].y) + sl[n][tbl][tal];
+                Rr[n] = (sb[n][tb][ta].x + sb[n][tb][ta].y) + sr[n][tb][ta];
+            }
+            // jumps from split parts: centre difference from the pairs, plus
+            // the difference of the FP32 perturbations
+            auto jump = [&](int n) {
+                return ((sb[n][tb][ta].x - sb[n][tbl][tal].x) + (sb[n][tb][ta].y - sb[n][tbl][tal].y))
+                       + (sr[n][tb][ta] - sl[n][tbl][tal]);
+            };
+            const float jv = jump(1);
+            const float jp = jump(6) + 0.5f * (jump(4) * (Rr[4] + L[4]) + jump(5) * (Rr[5] + L[5]));
+            const float bn = FI(SF_BF, 2);
+            const float dv0 = (sb[1][tb][ta].x - sb[1][tbl][tal].x) + (sb[1][tb][ta].y - sb[1][tbl][tal].y);
+            const float dvtm = fminf(fminf(FI(SF_DVT, 1), FI(SF_DVT, 2)),
+                                     fminf(FI(SF_DVU, 1), FI(SF_DVU, 2)));
+            float F[7];
+            riemann_jumps(which, L, Rr, bn, gamma, dv0, dvtm, F, jp, jv);
+            const float fct = 0.5f * (sl[7][tbl][tal] + sr[7][tb][ta]);
+            const float fcu = 0.5f * (sl[8][tbl][tal] + sr[8][tb][ta]);
+            F[4] -= fct;
+            F[5] -= fcu;
+            const long long c = d.ap(i, j, k);
+#pragma unroll
+            for (int n = 0; n < 7; n++) g.F[D][n][c] = F[n];
+            g.FC[D][0][c] = fct;
+            g.FC[D][1][c] = fcu;
+        }
+        __syncthreads();  // the stage and the per-cell results are reused
     }
-    // jumps from split parts: centre difference from the pairs, plus the
-    // difference of the FP32 perturbations
-    auto jump = [&](int n) {
-        return ((sb[n][tb][ta].x - sb[n][tbl][tal].x) + (sb[n][tb][ta].y - sb[n][tbl][tal].y))
-               + (sr[n][tb][ta] - sl[n][tbl][tal]);
-    };
-    const float jv = jump(1);
-    const float jp = jump(6) + 0.5f * (jump(4) * (Rr[4] + L[4]) + jump(5) * (Rr[5] + L[5]));
-    const float bn = v.bface[c];
-    const float dv0 = (sb[1][tb][ta].x - sb[1][tbl][tal].x) + (sb[1][tb][ta].y - sb[1][tbl][tal].y);
-    const float dvtm = fminf(fminf(v.dvt[c - st], v.dvt[c]), fminf(v.dvu[c - st], v.dvu[c]));
-    float F[7];
-    riemann_jumps(which, L, Rr, bn, gamma, dv0, dvtm, F, jp, jv);
-    const float fct = 0.5f * (sl[7][tbl][tal] + sr[7][tb][ta]);
-    const float fcu = 0.5f * (sl[8][tbl][tal] + sr[8][tb][ta]);
-    F[4] -= fct;
-    F[5] -= fcu;
-#pragma unroll
-    for (int n = 0; n < 7; n++) g.F[D][n][c] = F[n];
-    g.FC[D][0][c] = fct;
-    g.FC[D][1][c] = fcu;
 }
 
 // --- edge EMFs (FP32) --------------------------------------------------------
@@ -287,12 +418,12 @@ __device__ __forceinline__ float emf_part32(const float *fu, const float *fc, fl
     return h * ((ul0 + ur0) + w * (ul1 + ur1));
 }
 
-__global__ void __launch_bounds__(256) ks_emf(SplitFields g, Dims d, int odr)
+__global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= d.nx) return;
-    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
-    const long long c = d.at(i, j, k);
+    const long long sy = d.px, sz = d.px * d.ny;
+    const long long c = d.ap(i, j, k);
     const bool xi = (i >= 3 && i < d.nx - 2), yj = (j >= 3 && j < d.ny - 2),
                zk = (k >= 3 && k < d.nz - 2);
     float ez = 0.f, ex = 0.f, ey = 0.f;
@@ -335,32 +466,32 @@ __device__ __forceinline__ double df64(int odr, const float *f, long long s, lon
 }
 
 __global__ void __launch_bounds__(256)
-ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, float dtdx,
+ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, double ra, double rb, float dtdx,
           float dtdy, float dtdz, double dtdx_d, double dtdy_d, double dtdz_d)
 {
     const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = d.oy + blockIdx.y, k = d.oz + blockIdx.z;
     if (i >= d.nx - d.ox) return;
-    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
-    const long long s = d.at(i, j, k);
+    const long long sy = d.px, sz = d.px * d.ny;  // scratch strides
+    const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
     const int cX[5] = {0, 1, 2, 3, 6}, cY[5] = {0, 3, 1, 2, 6}, cZ[5] = {0, 2, 3, 1, 6};
     double out[8];
 #pragma unroll
     for (int v = 0; v < 5; v++) {
-        const float div = dtdx * df32(odr, g.F[0][cX[v]], s, 1) + dtdy * df32(odr, g.F[1][cY[v]], s, sy)
-                          + dtdz * df32(odr, g.F[2][cZ[v]], s, sz);
+        const float div = dtdx * df32(odr, g.F[0][cX[v]], sp, 1) + dtdy * df32(odr, g.F[1][cY[v]], sp, sy)
+                          + dtdz * df32(odr, g.F[2][cZ[v]], sp, sz);
         out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - (double)div);
     }
     // CT curl in FP64: the differences of the FP32 edge EMFs are exact in
     // FP64, so the discrete divergence of the B increment cancels to FP64
     // round-off (in FP32, 27*(E2-E1) alone would need more than 24 bits).
     const double ddx = (double)dtdx_d, ddy = (double)dtdy_d, ddz = (double)dtdz_d;
-    out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - ddy * df64(odr, g.e[2], s, sy)
-                                     + ddz * df64(odr, g.e[1], s, sz));
-    out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - ddz * df64(odr, g.e[0], s, sz)
-                                     + ddx * df64(odr, g.e[2], s, 1));
-    out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - ddx * df64(odr, g.e[1], s, 1)
-                                     + ddy * df64(odr, g.e[0], s, sy));
+    out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - ddy * df64(odr, g.e[2], sp, sy)
+                                     + ddz * df64(odr, g.e[1], sp, sz));
+    out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - ddz * df64(odr, g.e[0], sp, sz)
+                                     + ddx * df64(odr, g.e[2], sp, 1));
+    out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - ddx * df64(odr, g.e[1], sp, 1)
+                                     + ddy * df64(odr, g.e[0], sp, sy));
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
     const int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -379,13 +510,6 @@ ks_update(PlainFields f, SplitFields g, Dims d, int odr, double ra, double rb, f
     }
 }
 
-View make_view(const SplitFields &g, int D)
-{
-    if (D == 0) return {g.q[1], g.q[2], g.q[3], g.q[4], g.q[5], g.q[6], g.bf[0], g.dv[1], g.dv[2]};
-    if (D == 1) return {g.q[2], g.q[3], g.q[1], g.q[5], g.q[6], g.q[4], g.bf[1], g.dv[2], g.dv[0]};
-    return {g.q[3], g.q[1], g.q[2], g.q[6], g.q[4], g.q[5], g.bf[2], g.dv[0], g.dv[1]};
-}
-
 int falloc(Sim *s, float **p, long long n)
 {
     double *q = nullptr;
@@ -394,26 +518,147 @@ int falloc(Sim *s, float **p, long long n)
     return rc;
 }
 
+// Arrays staged by sweep D, in SQ_* / SF_* order.
+void sweep_arrays(const SplitPtrs &g, int D, const void *q[NQ], const void *f[NF])
+{
+    static const int vq[3][NQ] = {{0, 1, 2, 3, 5, 6, 7, 4}, {0, 2, 3, 1, 6, 4, 7, 5},
+                                  {0, 3, 1, 2, 4, 5, 7, 6}};
+    static const int dvt[3] = {1, 2, 0}, dvu[3] = {2, 0, 1};
+    for (int n = 0; n < NQ; n++) q[n] = g.q[vq[D][n]];
+    f[SF_M2] = g.m2;
+    f[SF_BF] = g.bf[D];
+    f[SF_DVT] = g.dv[dvt[D]];
+    f[SF_DVU] = g.dv[dvu[D]];
+}
+
+template <int D> int setup_sweep(Sim *s, SplitFields &sf)
+{
+    const Geometry &G = s->g;
+    constexpr int T = SG<D>::T;
+    const void *q[NQ], *f[NF];
+    sweep_arrays(sf.p, D, q, f);
+    for (int n = 0; n < NQ; n++) {
+        int rc = tma_map_3d(&sf.maps[D].q[n], q[n], sizeof(float2), G.nx, G.ny, G.nz, sf.px,
+                            SG<D>::BX, SG<D>::BY, SG<D>::BZ);
+        if (rc) return rc;
+    }
+    for (int n = 0; n < NF; n++) {
+        int rc = tma_map_3d(&sf.maps[D].f[n], f[n], sizeof(float), G.nx, G.ny, G.nz, sf.px,
+                            SG<D>::BX, SG<D>::BY, SG<D>::BZ);
+        if (rc) return rc;
+    }
+    int n0, n1, n2;
+    if (D == 0) {
+        n0 = (int)blocks_for(G.nx - 5, T - 1);
+        n1 = (int)blocks_for(G.ny, SG<0>::TB);
+        n2 = G.nz;
+    } else if (D == 1) {
+        n0 = (int)blocks_for(G.nx, SG<1>::TA);
+        n1 = (int)blocks_for(G.ny - 5, T - 1);
+        n2 = G.nz;
+    } else {
+        n0 = (int)blocks_for(G.nx, SG<2>::TA);
+        n1 = (int)blocks_for(G.nz - 5, T - 1);
+        n2 = G.ny;
+    }
+    sf.ntile[D][0] = n0;
+    sf.ntile[D][1] = n1;
+    sf.ntiles[D] = n0 * n1 * n2;
+    const size_t dyn = sweep_dyn_smem<D>();
+    MLAU_CUDA(cudaFuncSetAttribute(ks_sweep<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)dyn));
+    int dev = 0, sms = 0, per_sm = 0;
+    MLAU_CUDA(cudaGetDevice(&dev));
+    MLAU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MLAU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks_sweep<D>,
+                                                            SG<D>::TA * SG<D>::TB, dyn));
+    if (per_sm < 1) {
+        set_error("FP32-split sweep %d does not fit on an SM", D);
+        return MLAU_ERR_CUDA;
+    }
+    sf.nblocks[D] = std::max(1, std::min(sf.ntiles[D], sms * per_sm));
+    return MLAU_OK;
+}
+
+template <int D>
+void launch_sweep(Sim *s, SplitFields &sf, const Dims &d, float gam)
+{
+    const dim3 b(SG<D>::TA, SG<D>::TB);
+    ks_sweep<D><<<sf.nblocks[D], b, sweep_dyn_smem<D>(), s->stream>>>(
+        sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1], sf.ntiles[D],
+        sf.d_err);
+}
+
 }  // namespace
+
+int tma_map_3d(CUtensorMap *map, const void *base, int elem_bytes, int nx, int ny, int nz,
+               long long px, int bx, int by, int bz)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        MLAU_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                   cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return MLAU_ERR_CUDA;
+        }
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const long long row = px * elem_bytes;
+    if (((uintptr_t)base & 15) || (row & 15) || ((long long)bx * elem_bytes) % 16) {
+        set_error("tensor map: base, row pitch or box width not 16-byte aligned");
+        return MLAU_ERR_ARG;
+    }
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)row, (cuuint64_t)(row * ny)};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUtensorMapDataType ty =
+        elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_INT64 : CU_TENSOR_MAP_DATA_TYPE_INT32;
+    const CUresult r = encode(map, ty, 3, const_cast<void *>(base), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return MLAU_ERR_CUDA;
+    }
+    return MLAU_OK;
+}
 
 int split3d_alloc(Sim *s)
 {
     if (s->g.dim != 3) { set_error("FP32-split mode is 3D only"); return MLAU_ERR_ARG; }
     PlainFields &f = s->f;
-    const long long n = s->g.n;
+    const Geometry &G = s->g;
+    const long long n = G.n;
     int rc = 0;
     for (int v = 0; v < 8; v++) rc |= dalloc(s, &f.s[v], n) | dalloc(s, &f.u0[v], n);
     s->sp = new SplitFields();
-    SplitFields &g = *s->sp;
-    for (int v = 0; v < 8; v++) rc |= dalloc(s, (double **)&g.q[v], n);
-    for (int D = 0; D < 3; D++) rc |= falloc(s, &g.bf[D], n);
+    SplitFields &sf = *s->sp;
+    sf.px = (G.nx + 3) / 4 * 4;
+    const long long np = sf.px * G.ny * G.nz;
+    SplitPtrs &g = sf.p;
+    for (int v = 0; v < 8; v++) rc |= dalloc(s, (double **)&g.q[v], np);
+    for (int D = 0; D < 3; D++) rc |= falloc(s, &g.bf[D], np);
     for (int D = 0; D < 3; D++) {
-        for (int v = 0; v < 7; v++) rc |= falloc(s, &g.F[D][v], n);
-        rc |= falloc(s, &g.FC[D][0], n) | falloc(s, &g.FC[D][1], n);
-        rc |= falloc(s, &g.e[D], n) | falloc(s, &g.ct[D], n) | falloc(s, &g.dv[D], n);
+        for (int v = 0; v < 7; v++) rc |= falloc(s, &g.F[D][v], np);
+        rc |= falloc(s, &g.FC[D][0], np) | falloc(s, &g.FC[D][1], np);
+        rc |= falloc(s, &g.e[D], np) | falloc(s, &g.ct[D], np) | falloc(s, &g.dv[D], np);
     }
-    rc |= falloc(s, &g.m2, n);
-    return rc ? MLAU_ERR_NOMEM : MLAU_OK;
+    rc |= falloc(s, &g.m2, np);
+    double *flag = nullptr;
+    rc |= dalloc(s, &flag, 1);
+    if (rc) return MLAU_ERR_NOMEM;
+    sf.d_err = (int *)flag;
+    MLAU_CUDA(cudaMemset(sf.d_err, 0, sizeof(int)));
+    // the sweeps read the arrays' ghost rows too: start from zeros
+    for (int v = 0; v < 8; v++) MLAU_CUDA(cudaMemset(g.q[v], 0, sizeof(float2) * np));
+    int r2 = setup_sweep<0>(s, sf);
+    if (!r2) r2 = setup_sweep<1>(s, sf);
+    if (!r2) r2 = setup_sweep<2>(s, sf);
+    return r2;
 }
 
 void split3d_free(Sim *s)
@@ -422,13 +667,28 @@ void split3d_free(Sim *s)
     s->sp = nullptr;
 }
 
+// MLAU_ERR_TIMEOUT when a sweep gave up waiting for its staged tile (the
+// stream must be idle).
+int split3d_check(Sim *s)
+{
+    if (!s->sp || !s->sp->d_err) return MLAU_OK;
+    int e = 0;
+    MLAU_CUDA(cudaMemcpy(&e, s->sp->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        set_error("FP32-split sweep: a bounded wait for a staged tile gave up");
+        return MLAU_ERR_TIMEOUT;
+    }
+    return MLAU_OK;
+}
+
 int split3d_step(Sim *s, double dt)
 {
     const Geometry &G = s->g;
     PlainFields &f = s->f;
-    SplitFields &g = *s->sp;
+    SplitFields &sf = *s->sp;
+    SplitPtrs &g = sf.p;
     cudaStream_t st = s->stream;
-    const Dims d{G.nx, G.ny, G.nz, G.ox, G.oy, G.oz};
+    const Dims d{G.nx, G.ny, G.nz, G.ox, G.oy, G.oz, sf.px};
     {
         TimedLaunch tl(&s->timer, KK_COPY);
         for (int v = 0; v < 8; v++)
@@ -450,24 +710,9 @@ int split3d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_SWEEP);
-            {
-                constexpr int T = Tile<0>::TA;
-                dim3 b(Tile<0>::TA, Tile<0>::TB);
-                dim3 gr(blocks_for(G.nx - 5, T - 1), blocks_for((long long)G.ny * G.nz, Tile<0>::TB));
-                ks_sweep<0><<<gr, b, 0, st>>>(g, make_view(g, 0), d, s->odr, s->flux, gam);
-            }
-            {
-                constexpr int T = Tile<1>::TB;
-                dim3 b(Tile<1>::TA, Tile<1>::TB);
-                dim3 gr(blocks_for(G.nx, Tile<1>::TA), blocks_for(G.ny - 5, T - 1), G.nz);
-                ks_sweep<1><<<gr, b, 0, st>>>(g, make_view(g, 1), d, s->odr, s->flux, gam);
-            }
-            {
-                constexpr int T = Tile<2>::TB;
-                dim3 b(Tile<2>::TA, Tile<2>::TB);
-                dim3 gr(blocks_for(G.nx, Tile<2>::TA), blocks_for(G.nz - 5, T - 1), G.ny);
-                ks_sweep<2><<<gr, b, 0, st>>>(g, make_view(g, 2), d, s->odr, s->flux, gam);
-            }
+            launch_sweep<0>(s, sf, d, gam);
+            launch_sweep<1>(s, sf, d, gam);
+            launch_sweep<2>(s, sf, d, gam);
         }
         {
             TimedLaunch tl(&s->timer, KK_EMF);

@@ -150,6 +150,46 @@ def test_2d_many_steps(port):
     assert ics.div_b_2d(got, m["dx"], m["dy"]) <= 1e-12
 
 
+def test_3d_1000_steps_with_cfl_dt(port):
+    """1000 RK3 steps of the 3D driver's time loop (CFL dt every step) against
+    the oracle: equal values (budget: rel. L-inf 1e-9), div B at round-off."""
+    st, m = ics.turbulence_3d(n=12, mach=0.3, seed=21)
+    ref = ics.copy_state(st)
+    dr = min(m["dx"], m["dy"], m["dz"])
+    with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"], flux="mlau") as s:
+        s.upload(st)
+        dt_g = dt_c = 0.0
+        for n in range(1000):
+            dt_g, _ = s.cfl(0.4, dr, m["vfast"], dt_g)
+            dt_c = port.cfl3d(ref, 0.4, dr, m["vfast"], dt_c)[0]
+            assert dt_g == dt_c, n
+            s.step(dt_g, 1)
+            port.step3d(ref, dt_c, m["dx"], m["dy"], m["dz"], flux="mlau")
+        got = s.download()
+    assert max_rel_diff(got, ref) <= 1e-9
+    assert equal_values(got, ref), max_rel_diff(got, ref)
+    assert ics.div_b_3d(got, m["dx"], m["dy"], m["dz"]) <= 1e-12
+
+
+def test_2d_1000_steps_with_cfl_dt(port):
+    st, m = ics.turbulence_2d(n=32, ny=24, seed=22, vrms=0.8)
+    ref = ics.copy_state(st)
+    dr = min(m["dx"], m["dy"])
+    with M.Sim(2, st["ro"].shape, dx=m["dx"], dy=m["dy"], flux="lhlld") as s:
+        s.upload(st)
+        dt_g = dt_c = 0.0
+        for n in range(1000):
+            dt_g, _ = s.cfl(0.4, dr, 0.0, dt_g)
+            dt_c = port.cfl2d(ref, 0.4, dr, 0.0, dt_c)[0]
+            assert dt_g == dt_c, n
+            s.step(dt_g, 1)
+            port.step2d(ref, dt_c, m["dx"], m["dy"], flux="lhlld")
+        got = s.download()
+    assert max_rel_diff(got, ref) <= 1e-9
+    assert equal_values(got, ref), max_rel_diff(got, ref)
+    assert ics.div_b_2d(got, m["dx"], m["dy"]) <= 1e-12
+
+
 # --- CFL reduction -------------------------------------------------------------
 def test_cfl_3d(port):
     st, m = ics.turbulence_3d(n=16, mach=0.6, seed=4)
