@@ -155,8 +155,8 @@ def launch_flops(kind, n, off, opc, precision):
         return c["rec_per_cell"] * (N - 4) * N * N
     if kind == "flux":
         return c["flux_per_face"] * (N - 5) * N * N
-    if kind == "split_sweep":
-        return (c["rec_per_cell"] * (N - 4) + c["flux_per_face"] * (N - 5)) * N * N
+    if kind == "split_sweep":  # one timed launch = the three direction sweeps of a stage
+        return 3 * (c["rec_per_cell"] * (N - 4) + c["flux_per_face"] * (N - 5)) * N * N
     return None
 
 
@@ -196,14 +196,12 @@ def roofline(timing, n, off, peaks, precision):
 
 
 # --- our arm -----------------------------------------------------------------
-def run_ours(args, R: Ranks):
+def run_ours(args, R: Ranks, precision, st, meta):
     import mlau_gb300 as M
-    from mlau_gb300 import ics
 
     M.set_device(R.local)
     n, off = args.n, 4
-    st, meta = ics.turbulence_3d(n=n, mach=args.mach, seed=1000 + R.rank)
-    prec = M.FP32_SPLIT if args.precision == "split" else M.FP64
+    prec = M.FP32_SPLIT if precision == "split" else M.FP64
     sim = M.Sim(3, st["ro"].shape, off=off, dx=meta["dx"], dy=meta["dy"], dz=meta["dz"],
                 gamma=meta["gamma"], odr=4, flux="mlau", nrk=3, precision=prec)
     sim.upload(st)
@@ -230,8 +228,16 @@ def run_ours(args, R: Ranks):
               "device_bytes": sim.device_bytes}
     # end to end through the C ABI drop-in driver with pinned host buffers
     result["e2e"] = run_e2e(args, R, st, meta, dt, M, prec)
+    result["final"] = sim.download()
     sim.close()
     return result
+
+
+def rel_l1(a, b, off=4):
+    """Relative L1 difference of a against b over the interior, per variable."""
+    core = (slice(off, -off),) * 3
+    return {k: float(np.abs(a[k][core] - b[k][core]).sum() / np.abs(b[k][core]).sum())
+            for k in VARS}
 
 
 def run_e2e(args, R, st, meta, dt, M, prec):
@@ -314,6 +320,98 @@ def run_reference(args, R: Ranks):
     print(json.dumps(line), flush=True)
 
 
+# --- batched 2D and serving workloads ------------------------------------------
+def batch2d_requests(n_inst, seed, n2d=(64, 1024), t_end=(0.05, 0.5)):
+    """256 uneven periodic 2D instances: sizes log-uniform per axis, solver and
+    gamma uniform, rms Mach U[1e-3, 2], beta log-uniform in [0.1, 10]."""
+    from mlau_gb300 import serve
+    return serve.make_requests(n_inst, rate=1.0, seed=seed, mix=(0.0, 1.0, 0.0), n2d=n2d,
+                               t_end_2d=t_end, split_frac=1.0)
+
+
+def run_batch2d(args):
+    """Batched 2D engine, FP32-split: all instances in one persistent
+    cooperative launch per step, tile shape from the autotuner, steps replayed
+    from captured graphs; zone-updates/s over the instances still running."""
+    import mlau_gb300 as M
+    reqs = batch2d_requests(args.batch_n, seed=5)
+    cells = sum(r.state["ro"].size for r in reqs)
+    b = M.Batch.open(cells, len(reqs), precision=M.FP32_SPLIT, odr=4)
+    slots = [b.add(r.state, r.meta["dx"], r.meta["dy"], r.meta["gamma"], r.meta["flux"],
+                   r.meta["cfl"], r.meta["t_end"]) for r in reqs]
+    tw, th, tune_ms = b.autotune(steps=2)
+    b.run(args.warmup, steps_per_graph=args.warmup)
+    before = [b.info(s)[1] for s in slots]
+    active = sum(b.info(s)[2] for s in slots)
+    with ClockSampler(0) as clk:
+        left, ms = b.run(args.steps, steps_per_graph=args.steps)
+    # zone-updates actually done: instances that retire mid-run stop counting
+    zones = sum(r.interior * (b.info(s)[1] - n0) for r, s, n0 in zip(reqs, slots, before))
+    failed = sum(b.failed(s) for s in slots)
+    v = zones / (ms * 1e-3)
+    b.close()
+    return {"metric": "batched 2D zone-updates/s (uneven instances, one persistent launch per "
+                      "step, FP32-split)",
+            "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"{len(reqs)} periodic 2D instances, sizes log-uniform "
+                                   f"64..1024 per axis, solver/gamma uniform, Mach U[1e-3,2], "
+                                   f"beta logU[0.1,10], WCNS4 + CT + RK3, own CFL dt",
+                       "zone_updates": zones, "instances_active_at_start": active,
+                       "instances_active_at_end": left,
+                       "tile": [tw, th], "autotune_ms": tune_ms,
+                       "graph_steps": args.steps, "failed_instances": failed,
+                       "l2": "working set >> 129 MB L2"},
+            "gpu_launches": args.steps, "clocks": clk.summary()}
+
+
+def run_serve(args):
+    """Serving (continuous batching under an HBM budget) against solving the
+    same requests one at a time with the plain FP64 path, at several arrival
+    rates; time-to-solution counts from each request's arrival."""
+    import mlau_gb300 as M
+    from mlau_gb300 import serve
+    rates = [float(x) for x in args.rates.split(",")]
+    kw = dict(seed=11, n1d=(256, args.serve_n1d_max), n2d=(64, args.serve_n2d_max),
+              n3d=(64, args.serve_n3d_max), t_end_2d=(0.05, args.serve_t_end_max))
+    base = serve.make_requests(args.serve_n, rate=rates[0], **kw)
+    # one-at-a-time FP64 baseline: execution time of each request, measured once
+    execs, zu_serial = [], 0
+    for r in base:
+        _, steps, sec = serve.solve_alone_fp64(r)
+        execs.append(sec)
+        zu_serial += r.interior * steps
+    out = {"metric": "serving time-to-solution p50/p99 and zone-updates/s",
+           "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "f64 | f32+f64",
+           "data": "synthetic seeded Poisson request stream",
+           "config": {"workload": f"{args.serve_n} requests: 50% 1D Riemann N logU[256,16384], "
+                                  f"40% 2D periodic (sizes logU 64..1024, t_end U[0.05,0.5]), "
+                                  f"10% 3D periodic 64^3..128^3 x 200 steps; FP64 or FP32-split "
+                                  f"per request (1D in FP64)",
+                      "budget_gb": args.budget_gb,
+                      "ranges": {k: list(v) for k, v in kw.items() if k != "seed"}},
+           "rates": {}}
+    for rate in rates:
+        reqs = serve.make_requests(args.serve_n, rate=rate, **kw)
+        lat_s, end_s = serve.serial_schedule(reqs, execs)
+        with serve.Server(budget_bytes=args.budget_gb * 1e9) as srv:
+            done = srv.run(reqs, realtime=True)
+            makespan = max(r.t_done for r in done)
+        zu = sum(r.zone_updates for r in done)
+        out["rates"][str(rate)] = {
+            "served": serve.summary([r.latency for r in done], zu, makespan),
+            "one_at_a_time_fp64": serve.summary(lat_s, zu_serial, end_s),
+            "failed": sum(r.failed for r in done),
+            "by_kind_p50_s": {k: float(np.percentile([r.latency for r in done if r.kind == k], 50))
+                              for k in ("1d", "2d", "3d") if any(r.kind == k for r in done)},
+        }
+    head = out["rates"][str(rates[-1])]["served"]
+    out["value"] = head["p99_s"]
+    out["p50_s"], out["p99_s"] = head["p50_s"], head["p99_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,9 +420,19 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--mach", type=float, default=1e-2)
-    ap.add_argument("--precision", choices=("fp64", "split"), default="fp64")
+    ap.add_argument("--precision", choices=("both", "fp64", "split"), default="both",
+                    help="both: FP32-split is the headline value, FP64 beside it")
+    ap.add_argument("--workload", choices=("step3d", "batch2d", "serve"), default="step3d")
     ap.add_argument("--ref-n", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=256)
+    ap.add_argument("--serve-n", type=int, default=24)
+    ap.add_argument("--rates", default="5,50,200")
+    ap.add_argument("--budget-gb", type=float, default=120.0)
+    ap.add_argument("--serve-n1d-max", type=int, default=16384)
+    ap.add_argument("--serve-n2d-max", type=int, default=1024)
+    ap.add_argument("--serve-n3d-max", type=int, default=128)
+    ap.add_argument("--serve-t-end-max", type=float, default=0.5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     R = Ranks()
@@ -332,28 +440,52 @@ def main():
         if args.impl == "reference":
             run_reference(args, R)
             return
-        res = run_ours(args, R)
+        if args.workload == "batch2d":
+            if R.rank == 0:
+                print(json.dumps(run_batch2d(args)), flush=True)
+            return
+        if args.workload == "serve":
+            if R.rank == 0:
+                print(json.dumps(run_serve(args)), flush=True)
+            return
+        from mlau_gb300 import ics
+        st, meta = ics.turbulence_3d(n=args.n, mach=args.mach, seed=1000 + R.rank)
+        precs = ("split", "fp64") if args.precision == "both" else (args.precision,)
+        res = {p: run_ours(args, R, p, st, meta) for p in precs}
         if R.rank != 0:
             return
-        prec_name = "fp64" if args.precision == "fp64" else "fp32-split"
+        head = precs[0]
+        r = res[head]
+        prec_name = "fp64" if head == "fp64" else "fp32-split"
         line = {
-            "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": R.world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": R.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "dtype": "f64" if head == "fp64" else "f32+f64",
             "data": "synthetic (seeded random-phase ICs; no dataset in the reference)",
             "config": workload_desc(args.n, args.mach, prec_name) | {
                 "parallelism": f"replicas x{R.world}" if R.world > 1 else "single GPU",
-                "dt": res["dt"]},
-            "roofline": roofline(res["timing"], args.n, 4, res["peaks"], args.precision),
-            "e2e": res["e2e"],
-            "gpu_launches": res["launches"],
-            "clocks": res["clocks"],
-            "kernel_ms": {k: {"launches": c, "total_ms": t} for k, (c, t) in res["timing"].items()},
-            "peaks_measured": {"fp64_tflops": res["peaks"][0] / 1e12,
-                               "fp32_tflops": res["peaks"][1] / 1e12},
-            "device_bytes": res["device_bytes"],
+                "dt": r["dt"]},
+            "roofline": roofline(r["timing"], args.n, 4, r["peaks"], head),
+            "e2e": r["e2e"],
+            "gpu_launches": r["launches"],
+            "clocks": r["clocks"],
+            "kernel_ms": {k: {"launches": c, "total_ms": t} for k, (c, t) in r["timing"].items()},
+            "peaks_measured": {"fp64_tflops": r["peaks"][0] / 1e12,
+                               "fp32_tflops": r["peaks"][1] / 1e12},
+            "device_bytes": r["device_bytes"],
         }
+        if "fp64" in res and head != "fp64":
+            f = res["fp64"]
+            line["fp64"] = {
+                "value": f["value"], "ms_per_step": f["ms_per_step"], "e2e": f["e2e"],
+                "roofline": roofline(f["timing"], args.n, 4, f["peaks"], "fp64"),
+                "gpu_launches": f["launches"], "clocks": f["clocks"],
+                "kernel_ms": {k: {"launches": c, "total_ms": t}
+                              for k, (c, t) in f["timing"].items()}}
+            line["split_over_fp64"] = r["value"] / f["value"]
+            line["l1_vs_fp64"] = rel_l1(r["final"], f["final"]) | {
+                "after_steps": args.warmup + args.steps, "tolerance_ro": 1e-6}
         if not args.no_cpu_baseline and R.world == 1:
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line), flush=True)
