@@ -86,7 +86,12 @@ void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, dou
  * (dim = 1, 2 or 3).  Defaults are those of the shipped driver files:
  * 3D and 2D odr=2, nrk=3, LHLLD; 1D odr=1, nrk=2, LHLLD.  The environment
  * variables MLAU_ODR, MLAU_RK and MLAU_FLUX (mlau|lhlld|hlld|roe) override
- * the defaults at first use. */
+ * the defaults at first use.
+ * Reconstruction codes (odr): 1-4 as the drivers' ODR (1 first order,
+ * 2 MUSCL minmod, 3 WCNS3, 4 WCNS4); 5 and 6 are second-order MUSCL with the
+ * MC limiter (include/interp.h:45-51, the limiter of
+ * 2D/MPI/MRX/mhd_fd_ct_2d.c:107) and the Koren limiter (interp.h:61-72), the
+ * calc_flr alternatives the headers ship; everything else follows ODR 2. */
 int mlau_set_scheme(int dim, int odr, int flux, int nrk);
 int mlau_set_bc_1d(int bc);
 /* Arithmetic of the drop-in 3D driver: MLAU_FP64 (default; the reference's
@@ -105,7 +110,7 @@ typedef struct mlau_sim mlau_sim;
 
 /* dim 3: nx,ny,nz padded sizes; dim 2: nz = 1; dim 1: ny = nz = 1.
  * xoff/yoff/zoff: ghost depth (>= 3; the reference uses 4).  Interior width
- * must be at least the ghost depth.  odr 1..4, flux MLAU_FLUX_*, nrk 1..3,
+ * must be at least the ghost depth.  odr 1..6, flux MLAU_FLUX_*, nrk 1..3,
  * precision MLAU_FP64 or MLAU_FP32_SPLIT (3D only). */
 int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, int yoff,
                     int zoff, double dx, double dy, double dz, double gamma, int odr, int flux,

@@ -133,8 +133,8 @@ int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, i
     if (dim == 1) { ny = nz = 1; yoff = zoff = 0; }
     if (dim == 2) { nz = 1; zoff = 0; }
     if (!check_geometry(dim, nx, ny, nz, xoff, yoff, zoff)) return MLAU_ERR_ARG;
-    if (odr < 1 || odr > 4 || flux < 0 || flux > 3 || nrk < 1 || nrk > 3) {
-        set_error("scheme out of range (odr 1..4, flux 0..3, nrk 1..3)");
+    if (odr < 1 || odr > 6 || flux < 0 || flux > 3 || nrk < 1 || nrk > 3) {
+        set_error("scheme out of range (odr 1..6, flux 0..3, nrk 1..3)");
         return MLAU_ERR_ARG;
     }
     if (precision != MLAU_FP64 && !(precision == MLAU_FP32_SPLIT && dim == 3)) {
@@ -436,7 +436,7 @@ int mlau_set_scheme(int dim, int odr, int flux, int nrk)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     init_scheme();
-    if (dim < 1 || dim > 3 || odr < 1 || odr > 4 || flux < 0 || flux > 3 || nrk < 1 || nrk > 3) {
+    if (dim < 1 || dim > 3 || odr < 1 || odr > 6 || flux < 0 || flux > 3 || nrk < 1 || nrk > 3) {
         set_error("mlau_set_scheme: out of range");
         return MLAU_ERR_ARG;
     }

@@ -254,7 +254,7 @@ extern "C" {
 int mlau_batch_open(mlau_batch **out, int precision, long long capacity_cells, int max_inst,
                     int off, int odr)
 {
-    if (!out || capacity_cells <= 0 || max_inst <= 0 || off < 3 || odr < 1 || odr > 4 ||
+    if (!out || capacity_cells <= 0 || max_inst <= 0 || off < 3 || odr < 1 || odr > 6 ||
         (precision != MLAU_FP64 && precision != MLAU_FP32_SPLIT)) {
         set_error("batch: bad arguments");
         return MLAU_ERR_ARG;
@@ -320,7 +320,7 @@ int mlau_batch_open(mlau_batch **out, int precision, long long capacity_cells, i
 
 int mlau_batch1d_open(mlau_batch **out, long long capacity_cells, int max_inst, int off, int odr)
 {
-    if (!out || capacity_cells <= 0 || max_inst <= 0 || off < 4 || odr < 1 || odr > 4) {
+    if (!out || capacity_cells <= 0 || max_inst <= 0 || off < 4 || odr < 1 || odr > 6) {
         set_error("batch1d: bad arguments");
         return MLAU_ERR_ARG;
     }

@@ -55,6 +55,38 @@ template <class T> MLAU_HD void muscl_mm_lr(T f1, T f2, T f3, T &fl, T &fr)
     fr = f2 - df;
 }
 
+// minmod3 (funcs.h:39-43)
+template <class T> MLAU_HD T minmod3(T a, T b, T c)
+{
+    return vmin(vmax(vmax(a, b), c), T(0)) + vmax(vmin(vmin(a, b), c), T(0));
+}
+
+// interp.h:45-51: MUSCL with the MC limiter (alpha 2), the limiter of
+// 2D/MPI/MRX/mhd_fd_ct_2d.c:107
+template <class T> MLAU_HD void muscl_mc_lr(T f1, T f2, T f3, T &fl, T &fr)
+{
+    const T alpha = T(2.0);
+    T df = T(0.5) * minmod(alpha * minmod(f2 - f1, f3 - f2), T(0.5) * (f3 - f1));
+    fl = f2 + df;
+    fr = f2 - df;
+}
+
+// interp.h:61-72: MUSCL with the Koren limiter
+template <class T> MLAU_HD void muscl_kr_lr(T f1, T f2, T f3, T &fl, T &fr)
+{
+    const T d1 = T(2.0) * (f2 - f1);
+    const T d2 = T(2.0) * (f3 - f2);
+    const T dl = T(0.5) * minmod3(d1, d2, (T(0.5) * d1 + d2) / T(3.0));
+    const T dr = T(0.5) * minmod3(d1, d2, (d1 + T(0.5) * d2) / T(3.0));
+    fl = f2 + dl;
+    fr = f2 - dr;
+}
+
+// Reconstruction codes: 1-4 are the drivers' ODR; 5 and 6 are 2nd-order MUSCL
+// with the MC and Koren limiters in calc_flr's ODR 2 branch.  Every other
+// order-dependent operation follows ODR 2 for them.
+MLAU_HD int lin_odr(int odr) { return odr > 4 ? 2 : odr; }
+
 // interp.h:106-146
 template <class T> MLAU_HD void wcns3_lr(T f0, T f1, T f2, T &fl, T &fr)
 {
@@ -122,12 +154,15 @@ template <class T> MLAU_HD void rec_lr(int odr, const T *f, T &fl, T &fr)
     if (odr == 4) wcns4_lr(f[0], f[1], f[2], f[3], f[4], fl, fr);
     else if (odr == 2) muscl_mm_lr(f[1], f[2], f[3], fl, fr);
     else if (odr == 3) wcns3_lr(f[1], f[2], f[3], fl, fr);
+    else if (odr == 5) muscl_mc_lr(f[1], f[2], f[3], fl, fr);
+    else if (odr == 6) muscl_kr_lr(f[1], f[2], f[3], fl, fr);
     else { fl = f[2]; fr = f[2]; }
 }
 
 // lcal_flr (mhd_fd_ct_3d.c:48-63): linear face interpolation, left value.
 template <class T> MLAU_HD T lin_l(int odr, T f0, T f1, T f2, T f3, T f4)
 {
+    odr = lin_odr(odr);
     if (odr == 4)
         return T(0.003125) * (T(9.0) * f0 - T(56.0) * f1 + T(234.0) * f2 + T(144.0) * f3
                               - T(11.0) * f4);
@@ -138,6 +173,7 @@ template <class T> MLAU_HD T lin_l(int odr, T f0, T f1, T f2, T f3, T f4)
 // ... and the right value (mirror stencil).
 template <class T> MLAU_HD T lin_r(int odr, T f0, T f1, T f2, T f3, T f4)
 {
+    odr = lin_odr(odr);
     if (odr == 4)
         return T(0.003125) * (T(9.0) * f4 - T(56.0) * f3 + T(234.0) * f2 + T(144.0) * f1
                               - T(11.0) * f0);
@@ -149,14 +185,14 @@ template <class T> MLAU_HD T lin_r(int odr, T f0, T f1, T f2, T f3, T f4)
 // calc_bc (mhd_fd_ct_3d.c:38-46)
 template <class T> MLAU_HD T face2cen(int odr, T f0, T f1, T f2, T f3)
 {
-    if (odr <= 2) return T(0.5) * (f1 + f2);
+    if (lin_odr(odr) <= 2) return T(0.5) * (f1 + f2);
     return T(0.0625) * (T(9.0) * (f1 + f2) - (f0 + f3));
 }
 
 // calc_df (mhd_fd_ct_3d.c:80-88)
 template <class T> MLAU_HD T fdiff(int odr, T f0, T f1, T f2, T f3)
 {
-    if (odr <= 2) return f2 - f1;
+    if (lin_odr(odr) <= 2) return f2 - f1;
     return (T(27.0) * (f2 - f1) - (f3 - f0)) / T(24.0);
 }
 

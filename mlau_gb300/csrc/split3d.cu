@@ -61,7 +61,7 @@ struct SplitPtrs {
     float *bf[3];    // face-centred bx, by, bz rounded to FP32
     float *F[3][7];
     float *FC[3][2];
-    float *e[3];
+    double *e[3];    // edge EMFs (FP32 values held in FP64 for the CT curl)
     float *m2;
     float *ct[3];
     float *dv[3];
@@ -95,14 +95,55 @@ struct Dims {
 };
 
 // --- primitives (FP64 recovery, FP32-pair output) ------------------------
-__device__ __forceinline__ float2 split2(double x)
+// FP64 <-> FP32 conversions run on the FP64 pipe, which on this part is the
+// step's bottleneck; the helpers below do the common cases with integer bit
+// operations (exact IEEE field arithmetic) and fall back to the native
+// conversion for zero, tiny, huge and non-finite values.
+__device__ __forceinline__ float2 split2_native(double x)
 {
     const float h = (float)x;
     return make_float2(h, (float)(x - (double)h));
 }
 
+// x = hi + lo with hi the top 24 significand bits of x (truncated) and lo the
+// remaining 29 bits rounded to FP32: |x - (hi + lo)| <= 2^-47 |x|.
+__device__ __forceinline__ float2 split2(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 949 || e > 1150) return split2_native(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    const float hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
+    // the low 29 bits carry weight 2^(e - 1075); that power of two is a normal float here
+    const float lo = (float)(unsigned)(m & 0x1FFFFFFFu) * __uint_as_float((unsigned)(e - 948) << 23);
+    return make_float2(hi, __uint_as_float(__float_as_uint(lo) | sign));
+}
+
+// FP64 -> FP32, truncating the significand (error below one FP32 ulp).
+__device__ __forceinline__ float to_f32(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 897 || e > 1150) return (float)x;
+    return __uint_as_float(((unsigned)(b >> 63) << 31) | ((unsigned)(e - 896) << 23) |
+                           (unsigned)((b & 0xFFFFFFFFFFFFFull) >> 29));
+}
+
+// FP32 -> FP64, exact.
+__device__ __forceinline__ double to_f64(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ef = (u >> 23) & 0xff;
+    if (ef == 0 || ef == 0xff) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u >> 31) << 63) |
+                                 ((unsigned long long)(ef + 896) << 52) |
+                                 ((unsigned long long)(u & 0x7fffff) << 29);
+    return __longlong_as_double((long long)b);
+}
+
 __global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, double gamma)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, double gamma, float gamma_f)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
     if (i >= d.nx) return;
@@ -118,24 +159,26 @@ ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, double gamma)
     // as an additive term, so its FP32 rounding (1e-7 of itself) stays below
     // the pressure's own FP32 resolution at any Mach number; the cancelling
     // terms E and B^2/2 stay FP64.
-    const float rof = (float)ro, irof = 1.0f / rof;
-    const float vx = (float)f.s[1][s] * irof, vy = (float)f.s[2][s] * irof,
-                vz = (float)f.s[3][s] * irof;
+    const float2 ro2 = split2(ro);
+    const float rof = ro2.x + ro2.y, irof = 1.0f / rof;
+    const float vx = to_f32(f.s[1][s]) * irof, vy = to_f32(f.s[2][s]) * irof,
+                vz = to_f32(f.s[3][s]) * irof;
     const float v2 = vx * vx + vy * vy + vz * vz;
     const double b2 = cx * cx + cy * cy + cz * cz;
-    const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * ((double)(rof * v2) + b2));
-    g.q[0][sp] = split2(ro);
+    const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * (to_f64(rof * v2) + b2));
+    const float2 pr2 = split2(pr);
+    g.q[0][sp] = ro2;
     g.q[1][sp] = make_float2(vx, 0.f);
     g.q[2][sp] = make_float2(vy, 0.f);
     g.q[3][sp] = make_float2(vz, 0.f);
     g.q[4][sp] = split2(cx);
     g.q[5][sp] = split2(cy);
     g.q[6][sp] = split2(cz);
-    g.q[7][sp] = split2(pr);
-    g.bf[0][sp] = (float)bx[s];
-    g.bf[1][sp] = (float)by[s];
-    g.bf[2][sp] = (float)bz[s];
-    g.m2[sp] = v2 / ((float)gamma * (float)pr * irof);
+    g.q[7][sp] = pr2;
+    g.bf[0][sp] = to_f32(bx[s]);
+    g.bf[1][sp] = to_f32(by[s]);
+    g.bf[2][sp] = to_f32(bz[s]);
+    g.m2[sp] = v2 / (gamma_f * (pr2.x + pr2.y) * irof);
 }
 
 // --- CT weights and shock sensors (FP32) ----------------------------------
@@ -442,9 +485,9 @@ __global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr)
         ey = emf_part32(g.F[0][5], g.FC[0][1], w, 0.5f, c, sz, odr)
              + emf_part32(g.F[2][4], g.FC[2][0], 1.f - w, -0.5f, c, 1, odr);
     }
-    g.e[0][c] = ex;
-    g.e[1][c] = ey;
-    g.e[2][c] = ez;
+    g.e[0][c] = to_f64(ex);
+    g.e[1][c] = to_f64(ey);
+    g.e[2][c] = to_f64(ez);
 }
 
 // --- RK combine + CT curl ------------------------------------------------------
@@ -456,13 +499,14 @@ __device__ __forceinline__ float df32(int odr, const float *f, long long s, long
     return fdiff(odr, f[s - st], f[s], f[s + st], f[s + 2 * st]);
 }
 
-// FP64 face-to-centre difference of FP32 edge EMFs; the 1/24 of the 4th-order
-// stencil is a multiplication here (no FP64 division).
-__device__ __forceinline__ double df64(int odr, const float *f, long long s, long long st)
+// FP64 difference of the (FP32-valued) edge EMFs along one axis, without the
+// 1/24 of the 4th-order stencil (folded into dt/dx by the caller): every
+// operation is exact, so the discrete divergence of the curl cancels.
+__device__ __forceinline__ double df64(int odr, const double *f, long long s, long long st)
 {
     const double f0 = f[s - st], f1 = f[s], f2 = f[s + st], f3 = f[s + 2 * st];
-    if (odr <= 2) return f2 - f1;
-    return (27.0 * (f2 - f1) - (f3 - f0)) * (1.0 / 24.0);
+    if (lin_odr(odr) <= 2) return f2 - f1;
+    return 27.0 * (f2 - f1) - (f3 - f0);
 }
 
 __global__ void __launch_bounds__(256)
@@ -480,12 +524,13 @@ ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, double ra, double rb, flo
     for (int v = 0; v < 5; v++) {
         const float div = dtdx * df32(odr, g.F[0][cX[v]], sp, 1) + dtdy * df32(odr, g.F[1][cY[v]], sp, sy)
                           + dtdz * df32(odr, g.F[2][cZ[v]], sp, sz);
-        out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - (double)div);
+        out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - to_f64(div));
     }
     // CT curl in FP64: the differences of the FP32 edge EMFs are exact in
     // FP64, so the discrete divergence of the B increment cancels to FP64
     // round-off (in FP32, 27*(E2-E1) alone would need more than 24 bits).
-    const double ddx = (double)dtdx_d, ddy = (double)dtdy_d, ddz = (double)dtdz_d;
+    // dtdx_d etc. carry the stencil's 1/24 when odr > 2.
+    const double ddx = dtdx_d, ddy = dtdy_d, ddz = dtdz_d;
     out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - ddy * df64(odr, g.e[2], sp, sy)
                                      + ddz * df64(odr, g.e[1], sp, sz));
     out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - ddz * df64(odr, g.e[0], sp, sz)
@@ -645,7 +690,7 @@ int split3d_alloc(Sim *s)
     for (int D = 0; D < 3; D++) {
         for (int v = 0; v < 7; v++) rc |= falloc(s, &g.F[D][v], np);
         rc |= falloc(s, &g.FC[D][0], np) | falloc(s, &g.FC[D][1], np);
-        rc |= falloc(s, &g.e[D], np) | falloc(s, &g.ct[D], np) | falloc(s, &g.dv[D], np);
+        rc |= dalloc(s, &g.e[D], np) | falloc(s, &g.ct[D], np) | falloc(s, &g.dv[D], np);
     }
     rc |= falloc(s, &g.m2, np);
     double *flag = nullptr;
@@ -705,7 +750,7 @@ int split3d_step(Sim *s, double dt)
         const double ra = t[rk][0], rb = t[rk][1];
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
-            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, s->gamma);
+            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, s->gamma, (float)s->gamma);
             ks_aux<<<cg, cb, 0, st>>>(g, d);
         }
         {
@@ -720,9 +765,10 @@ int split3d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_UPDATE);
+            const double c24 = lin_odr(s->odr) > 2 ? 1.0 / 24.0 : 1.0;
             ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, ra, rb, (float)(dt / G.dx),
-                                         (float)(dt / G.dy), (float)(dt / G.dz), dt / G.dx,
-                                         dt / G.dy, dt / G.dz);
+                                         (float)(dt / G.dy), (float)(dt / G.dz),
+                                         dt / G.dx * c24, dt / G.dy * c24, dt / G.dz * c24);
         }
         MLAU_CUDA(cudaGetLastError());
     }

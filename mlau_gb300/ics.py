@@ -73,7 +73,7 @@ def _ddx(f, axis, n, odr):
     index i uses f[i-1..i+2] (face-to-centre or edge-to-face), divided by 1/n."""
     f1 = f
     f2 = np.roll(f, -1, axis=axis)
-    if odr <= 2:
+    if odr <= 2 or odr > 4:  # 5, 6: MUSCL codes, 2nd-order differences
         d = f2 - f1
     else:
         f0 = np.roll(f, 1, axis=axis)
@@ -86,7 +86,7 @@ def _center(f, axis, odr):
     """Scheme face-to-centre average (calc_bc) of a periodic face field."""
     f1 = f
     f2 = np.roll(f, -1, axis=axis)
-    if odr <= 2:
+    if odr <= 2 or odr > 4:  # 5, 6: MUSCL codes, 2nd-order differences
         return 0.5 * (f1 + f2)
     f0 = np.roll(f, 1, axis=axis)
     f3 = np.roll(f, -2, axis=axis)
@@ -228,7 +228,7 @@ def div_b_3d(st, dx, dy, dz, off=4, odr=4):
     def d(f, ax, h):
         f1 = f
         f2 = np.roll(f, -1, axis=ax)
-        if odr <= 2:
+        if odr <= 2 or odr > 4:  # 5, 6: MUSCL codes, 2nd-order differences
             return (f2 - f1) / h
         f0, f3 = np.roll(f, 1, axis=ax), np.roll(f, -2, axis=ax)
         return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0 / h
@@ -242,7 +242,7 @@ def div_b_2d(st, dx, dy, off=4, odr=4):
     def d(f, ax, h):
         f1 = f
         f2 = np.roll(f, -1, axis=ax)
-        if odr <= 2:
+        if odr <= 2 or odr > 4:  # 5, 6: MUSCL codes, 2nd-order differences
             return (f2 - f1) / h
         f0, f3 = np.roll(f, 1, axis=ax), np.roll(f, -2, axis=ax)
         return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0 / h

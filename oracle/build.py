@@ -59,7 +59,19 @@ def _variant_name(dim: int, odr: int, flux: int, nrk: int, bc: str) -> str:
     return f"ref{dim}d_o{odr}_{FLUX_NAMES[flux]}_rk{nrk}" + (f"_{bc}" if dim == 1 else "")
 
 
+# reconstruction codes 5 and 6: ODR 2 with calc_flr's MUSCL limiter swapped
+# for the MC or Koren limiter of include/interp.h
+LIMITER_SWAP = {5: "muscl_mc_cal_flr", 6: "muscl_kr_cal_flr"}
+
+
 def _patch_driver(text: str, odr: int, flux: int, nrk: int) -> str:
+    if odr in LIMITER_SWAP:
+        text, n0 = re.subn(r"^(\s*)muscl_mm_cal_flr\(f\[1\],f\[2\],f\[3\],fl,fr\);",
+                           lambda m: f"{m.group(1)}{LIMITER_SWAP[odr]}(f[1],f[2],f[3],fl,fr);",
+                           text, count=1, flags=re.M)
+        if n0 != 1:
+            raise RuntimeError("reference calc_flr layout not recognised; limiter patch failed")
+        odr = 2
     text, n1 = re.subn(r"^#define ODR \(\d\)", f"#define ODR ({odr})", text, count=1, flags=re.M)
     text, n2 = re.subn(r"^#define R_K \(\d\)", f"#define R_K ({nrk})", text, count=1, flags=re.M)
     text, n3 = re.subn(r"^(\s*)func_flux=&calc_flux_lhlld;",
@@ -117,10 +129,15 @@ def all_variants():
                 yield dict(dim=dim, odr=odr, flux=flux, nrk=3)
         for nrk in (1, 2):
             yield dict(dim=dim, odr=4, flux=0, nrk=nrk)
+        for odr in (5, 6):
+            for flux in (0, 1):
+                yield dict(dim=dim, odr=odr, flux=flux, nrk=3)
     for bc in ("open", "periodic"):
         for odr in (1, 2, 3, 4):
             for flux in (0, 1, 2, 3):
                 yield dict(dim=1, odr=odr, flux=flux, nrk=3, bc=bc)
+        for odr in (5, 6):
+            yield dict(dim=1, odr=odr, flux=0, nrk=3, bc=bc)
 
 
 def build_ref_all(jobs: int = 8) -> list:

@@ -24,6 +24,39 @@ static inline void o_muscl_mm(double f1, double f2, double f3, double *fl, doubl
     *fr = f2 - df;
 }
 
+/* minmod3 (include/funcs.h:39-43). */
+static inline double o_minmod3(double a, double b, double c)
+{
+    return o_min(o_max(o_max(a, b), c), 0.0) + o_max(o_min(o_min(a, b), c), 0.0);
+}
+
+/* include/interp.h:45-51 (2nd-order MUSCL, MC limiter with alpha 2; the
+   limiter of 2D/MPI/MRX/mhd_fd_ct_2d.c:107). */
+static inline void o_muscl_mc(double f1, double f2, double f3, double *fl, double *fr)
+{
+    const double alpha = 2.0;
+    double df = 0.5 * o_minmod(alpha * o_minmod(f2 - f1, f3 - f2), 0.5 * (f3 - f1));
+    *fl = f2 + df;
+    *fr = f2 - df;
+}
+
+/* include/interp.h:61-72 (2nd-order MUSCL, Koren limiter). */
+static inline void o_muscl_kr(double f1, double f2, double f3, double *fl, double *fr)
+{
+    double d1 = 2.0 * (f2 - f1);
+    double d2 = 2.0 * (f3 - f2);
+    double dl = 0.5 * o_minmod3(d1, d2, (0.5 * d1 + d2) / 3.0);
+    double dr = 0.5 * o_minmod3(d1, d2, (d1 + 0.5 * d2) / 3.0);
+    *fl = f2 + dl;
+    *fr = f2 - dr;
+}
+
+/* Reconstruction codes: 1-4 are the drivers' ODR; 5 and 6 are 2nd-order
+   MUSCL with the MC and Koren limiters in calc_flr's ODR 2 branch (the
+   alternatives include/interp.h ships).  Every other order-dependent
+   operation (linear interpolation, calc_bc, calc_df) follows ODR 2 for them. */
+static inline int o_lin_odr(int odr) { return odr > 4 ? 2 : odr; }
+
 /* include/interp.h:106-146 (3rd-order WCNS, ESWENO3 weights). */
 static inline void o_wcns3(double f0, double f1, double f2, double *fl, double *fr)
 {
@@ -92,6 +125,8 @@ static inline void o_rec_lr(int odr, const double *f, double *fl, double *fr)
     case 1: *fl = f[2]; *fr = f[2]; break;
     case 2: o_muscl_mm(f[1], f[2], f[3], fl, fr); break;
     case 3: o_wcns3(f[1], f[2], f[3], fl, fr); break;
+    case 5: o_muscl_mc(f[1], f[2], f[3], fl, fr); break;
+    case 6: o_muscl_kr(f[1], f[2], f[3], fl, fr); break;
     default: o_wcns4(f[0], f[1], f[2], f[3], f[4], fl, fr); break;
     }
 }
@@ -99,7 +134,7 @@ static inline void o_rec_lr(int odr, const double *f, double *fl, double *fr)
 /* lcal_flr of the drivers (mhd_fd_ct_3d.c:48-63): linear face interpolation. */
 static inline void o_lin_lr(int odr, const double *f, double *fl, double *fr)
 {
-    switch (odr) {
+    switch (o_lin_odr(odr)) {
     case 1: *fl = f[2]; *fr = f[2]; break;
     case 2:
         *fl = 0.25 * (-f[1] + 4.0 * f[2] + f[3]);
@@ -119,14 +154,14 @@ static inline void o_lin_lr(int odr, const double *f, double *fl, double *fr)
 /* calc_bc (mhd_fd_ct_3d.c:38-46): face B to cell centre. */
 static inline double o_face2cen(int odr, double f0, double f1, double f2, double f3)
 {
-    if (odr <= 2) return 0.5 * (f1 + f2);
+    if (o_lin_odr(odr) <= 2) return 0.5 * (f1 + f2);
     return 0.0625 * (9.0 * (f1 + f2) - (f0 + f3));
 }
 
 /* calc_df (mhd_fd_ct_3d.c:80-88): face-to-centre first difference. */
 static inline double o_diff(int odr, double f0, double f1, double f2, double f3)
 {
-    if (odr <= 2) return f2 - f1;
+    if (o_lin_odr(odr) <= 2) return f2 - f1;
     return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0;
 }
 

@@ -1,7 +1,7 @@
 """Generate the golden vectors in this directory from the reference itself.
 
 Run here, where the reference tree is present:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names...]
 It compiles the reference's own drivers (oracle/build.py, from the reference
 sources) for each scheme variant, runs them on seeded inputs, and stores the
 inputs and outputs.  3D/2D states are stored as their interior cells only: the
@@ -32,6 +32,8 @@ CASES_3D = [  # (name, n, mach, odr, flux, seed)
     ("3d_mlau_o2", 8, 0.9, 2, "mlau", 5),
     ("3d_lhlld_o3", 8, 0.9, 3, "lhlld", 6),
     ("3d_mlau_o4_lowmach", 8, 1e-2, 4, "mlau", 7),
+    ("3d_mlau_o5", 8, 0.9, 5, "mlau", 8),
+    ("3d_lhlld_o6", 8, 0.9, 6, "lhlld", 9),
 ]
 CASES_2D = [
     ("2d_lhlld_o4", 16, 4, "lhlld", 1),
@@ -39,6 +41,8 @@ CASES_2D = [
     ("2d_hlld_o2", 16, 2, "hlld", 3),
     ("2d_roe_o4", 16, 4, "roe", 4),
     ("2d_lhlld_o1", 16, 1, "lhlld", 5),
+    ("2d_lhlld_o5", 16, 5, "lhlld", 6),
+    ("2d_mlau_o6", 16, 6, "mlau", 7),
 ]
 CASES_1D = [  # (name, n, odr, flux, bc, seed)
     ("1d_mlau_o2_open", 64, 2, "mlau", "open", 1),
@@ -46,6 +50,8 @@ CASES_1D = [  # (name, n, odr, flux, bc, seed)
     ("1d_hlld_o4_open", 64, 4, "hlld", "open", 3),
     ("1d_roe_o3_open", 64, 3, "roe", "open", 4),
     ("1d_mlau_o4_periodic", 64, 4, "mlau", "periodic", 5),
+    ("1d_mlau_o5_open", 64, 5, "mlau", "open", 6),
+    ("1d_lhlld_o6_periodic", 64, 6, "lhlld", "periodic", 7),
 ]
 STEPS = (1, 4)
 
@@ -54,8 +60,12 @@ def interior(a, dim):
     return np.ascontiguousarray(a[(slice(OFF, -OFF),) * dim])
 
 
-def main():
+def main(only=()):
+    """Write every case, or only the named ones (existing files are kept)."""
+    skip = (lambda name: bool(only) and name not in only)
     for name, n, mach, odr, flux, seed in CASES_3D:
+        if skip(name):
+            continue
         st, m = ics.turbulence_3d(n=n, mach=mach, seed=seed, odr=odr)
         dt = 0.3 * m["dx"] / m["vfast"]
         out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "odr": odr, "flux": flux}
@@ -71,6 +81,8 @@ def main():
                 out[f"out{nstep}_" + k] = interior(v, 3)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     for name, n, odr, flux, seed in CASES_2D:
+        if skip(name):
+            continue
         st, m = ics.turbulence_2d(n=n, seed=seed, odr=odr, vrms=1.2)
         dt = 0.3 * m["dx"] / m["vfast"]
         out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "odr": odr, "flux": flux}
@@ -86,6 +98,8 @@ def main():
                 out[f"out{nstep}_" + k] = interior(v, 2)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     for name, n, odr, flux, bc, seed in CASES_1D:
+        if skip(name):
+            continue
         st, m = ics.riemann_1d(n=n, seed=seed)
         from oracle import Port
         dt = Port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
@@ -102,8 +116,8 @@ def main():
             for k, v in s.items():
                 out[f"out{nstep}_" + k] = v.copy()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
-    print("wrote", len(CASES_3D) + len(CASES_2D) + len(CASES_1D), "golden cases to", HERE)
+    print("wrote golden cases to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

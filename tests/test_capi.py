@@ -65,7 +65,7 @@ def test_create_rejects_bad_geometry(gpu_lib):
 
 def test_set_scheme_validation(gpu_lib):
     L = gpu_lib.lib()
-    assert L.mlau_set_scheme(3, 5, 0, 3) == -1
+    assert L.mlau_set_scheme(3, 7, 0, 3) == -1
     assert L.mlau_set_scheme(3, 4, 9, 3) == -1
     assert L.mlau_set_bc_1d(7) == -1
 

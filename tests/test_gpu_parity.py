@@ -13,7 +13,7 @@ from mlau_gb300 import ics
 
 pytestmark = pytest.mark.gpu
 
-ORDERS = (1, 2, 3, 4)
+ORDERS = (1, 2, 3, 4, 5, 6)  # 5, 6: MUSCL with the MC / Koren limiter
 FLUXES = ("mlau", "lhlld", "hlld", "roe")
 
 

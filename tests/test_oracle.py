@@ -48,9 +48,14 @@ def test_port_matches_golden_1d(port, name):
 
 needs_ref = pytest.mark.skipif(not Ref.available(), reason="reference tree not present")
 
+# reconstruction codes 1-4 (ODR) with every solver; 5, 6 (MUSCL with the MC /
+# Koren limiter, built by swapping calc_flr's limiter call) with two solvers
+SCHEMES = (list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe")))
+           + list(itertools.product((5, 6), ("mlau", "lhlld"))))
+
 
 @needs_ref
-@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe"))))
+@pytest.mark.parametrize("odr,flux", SCHEMES)
 def test_port_matches_reference_3d(port, odr, flux):
     st, m = ics.turbulence_3d(n=6, ny=7, nz=5, mach=0.8, seed=odr * 7 + len(flux), odr=odr)
     # inconsistent ghosts: the step must read exactly the reference's cells
@@ -67,7 +72,7 @@ def test_port_matches_reference_3d(port, odr, flux):
 
 
 @needs_ref
-@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe"))))
+@pytest.mark.parametrize("odr,flux", SCHEMES)
 def test_port_matches_reference_2d(port, odr, flux):
     st, m = ics.turbulence_2d(n=20, ny=14, seed=odr + 3, odr=odr, vrms=1.3)
     a, b = ics.copy_state(st), ics.copy_state(st)
@@ -79,7 +84,7 @@ def test_port_matches_reference_2d(port, odr, flux):
 
 @needs_ref
 @pytest.mark.parametrize("bc", ("open", "periodic"))
-@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4), ("mlau", "lhlld", "hlld", "roe"))))
+@pytest.mark.parametrize("odr,flux", SCHEMES)
 def test_port_matches_reference_1d(port, odr, flux, bc):
     st, m = ics.riemann_1d(n=48, seed=odr * 5 + len(flux))
     dt = port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
