@@ -320,6 +320,105 @@ def run_reference(args, R: Ranks):
     print(json.dumps(line), flush=True)
 
 
+# --- 2D and 1D single-problem workloads ------------------------------------------
+def run_step2d(args):
+    """Config C1: 2D periodic box 512^2, LHLLD + WCNS4 + CT + SSP-RK3, FP64 plain
+    (bit-exact to the reference), gamma=5/3, random-phase ICs (v_rms 0.5,
+    beta 1); K steps at a fixed dt, device-resident, plus the CPU
+    restatement of the reference timed on a bounded sample beside it."""
+    import mlau_gb300 as M
+    from mlau_gb300 import ics
+    n = args.n2d
+    st, m = ics.turbulence_2d(n=n, seed=3, vrms=0.5)
+    dt = 0.4 * m["dx"] / m["vfast"]
+    peaks = M.measure_fma_peaks()
+    with M.Sim(2, st["ro"].shape, dx=m["dx"], dy=m["dy"], gamma=m["gamma"], odr=4,
+               flux="lhlld", nrk=3) as s:
+        s.upload(st)
+        s.step(dt, args.warmup)
+        s.sync()
+        s.set_timing(True)
+        with ClockSampler(0) as clk:
+            ms = s.time_steps(dt, args.steps)
+        timing = s.timing()
+        launches = s.launches_per_step * args.steps
+    v = n * n * args.steps / (ms * 1e-3)
+    opc = load_opcounts()["lhlld_wcns4_2d"]
+    N = n + 8
+    dom = max(timing, key=lambda k: timing[k][1])
+    cnt, tot = timing[dom]
+    fl = {"rec": opc["rec_per_cell"] * (N - 4) * N, "flux": opc["flux_per_face"] * (N - 5) * N}
+    roof = {"kernel": dom, "bound": "fp64", "unit": "TFLOP/s", "peak": peaks[0] / 1e12,
+            "peak_source": "live FMA-throughput probe (2 flop/FMA)", "traffic": None,
+            "avg_launch_ms": tot / cnt, "share_of_step": tot / sum(x[1] for x in timing.values())}
+    if dom in fl:
+        roof["achieved"] = fl[dom] / (tot / cnt * 1e-3) / 1e12
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    # CPU restatement of the reference on a bounded sample (same problem)
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    from oracle import Port
+    cst = ics.copy_state(st)
+    Port.step2d(cst, dt, m["dx"], m["dy"], odr=4, flux="lhlld")
+    t0 = time.perf_counter()
+    for _ in range(args.cpu_steps):
+        Port.step2d(cst, dt, m["dx"], m["dy"], odr=4, flux="lhlld")
+    cv = n * n * args.cpu_steps / (time.perf_counter() - t0)
+    return {"metric": "2D zone-updates/s per RK3 step", "value": v, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded random-phase ICs)",
+            "config": {"workload": f"2D periodic box {n}^2, LHLLD + WCNS4 + CT + SSP-RK3, "
+                                   "gamma=5/3, v_rms 0.5, beta 1, FP64 plain (bit-exact)",
+                       "l2": f"state 8 x {N * N * 8 / 1e6:.1f} MB fits in L2: steady-state "
+                             "throughput of a resident problem, no flush"},
+            "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(),
+            "kernel_ms": {k: {"launches": c, "total_ms": t} for k, (c, t) in timing.items()},
+            "cpu_baseline": {"value": cv, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port", "sample": f"{n}^2 x {args.cpu_steps} steps"}}
+
+
+def run_step1d(args):
+    """Config C0: 1D Riemann problem, 2048 cells, MLAU + MUSCL (minmod) + RK3,
+    gamma=2, CFL 0.4, open boundaries, dt fixed from the initial state, run to
+    t_end=0.1 as the 1D driver does; the whole run is timed (one problem is
+    launch-latency bound: 13 launches per step)."""
+    import mlau_gb300 as M
+    from mlau_gb300 import ics
+    from oracle import Port
+    st, m = ics.riemann_1d(n=2048, seed=0)
+    with M.Sim(1, st["ro"].shape, dx=m["dx"], gamma=m["gamma"], odr=2, flux="mlau", nrk=3) as s:
+        s.set_bx(m["bx"])
+        s.set_bc("open")
+        s.upload(st)
+        dt, _ = s.cfl(0.4, m["dx"], 1.0, 0.0)
+        t, nsteps = 0.0, 0
+        while t < 0.1:
+            t += dt
+            nsteps += 1
+        s.step(dt, args.warmup)
+        s.sync()
+        with ClockSampler(0) as clk:
+            ms = s.time_steps(dt, nsteps)
+        launches = s.launches_per_step * nsteps
+    v = 2048 * nsteps / (ms * 1e-3)
+    cst = ics.copy_state(st)
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        Port.step1d(cst, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=2, flux="mlau", nrk=3)
+    cv = 2048 * nsteps / (time.perf_counter() - t0)
+    return {"metric": "1D zone-updates/s per RK3 step (whole run to t_end)", "value": v,
+            "unit": UNIT, "n_gpus": 1, "steps": nsteps, "warmup": args.warmup,
+            "ms_per_step": ms / nsteps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Riemann states)",
+            "config": {"workload": "1D Riemann problem, 2048 cells, MLAU + MUSCL-minmod + RK3, "
+                                   "gamma=2, CFL 0.4, open boundaries, t_end 0.1",
+                       "time_to_solution_ms": ms, "l2": "fits in L2 (one resident problem)"},
+            "roofline": None, "roofline_note": "latency bound: 13 launches of ~2k threads per step",
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "cpu_baseline": {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"the whole run, {nsteps} steps"}}
+
+
 # --- batched 2D and serving workloads ------------------------------------------
 def batch2d_requests(n_inst, seed, n2d=(64, 1024), t_end=(0.05, 0.5)):
     """256 uneven periodic 2D instances: sizes log-uniform per axis, solver and
@@ -422,7 +521,10 @@ def main():
     ap.add_argument("--mach", type=float, default=1e-2)
     ap.add_argument("--precision", choices=("both", "fp64", "split"), default="both",
                     help="both: FP32-split is the headline value, FP64 beside it")
-    ap.add_argument("--workload", choices=("step3d", "batch2d", "serve"), default="step3d")
+    ap.add_argument("--workload", choices=("step3d", "step2d", "step1d", "batch2d", "serve"),
+                    default="step3d")
+    ap.add_argument("--n2d", type=int, default=512)
+    ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-n", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-n", type=int, default=256)
@@ -439,6 +541,11 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, R)
+            return
+        if args.workload in ("step2d", "step1d"):
+            if R.rank == 0:
+                fn = run_step2d if args.workload == "step2d" else run_step1d
+                print(json.dumps(fn(args)), flush=True)
             return
         if args.workload == "batch2d":
             if R.rank == 0:
