@@ -46,6 +46,8 @@ enum { MLAU_FLUX_MLAU = 0, MLAU_FLUX_LHLLD = 1, MLAU_FLUX_HLLD = 2, MLAU_FLUX_RO
 enum { MLAU_FP64 = 0, MLAU_FP32_SPLIT = 1 };
 /* 1D boundaries. */
 enum { MLAU_BC1D_OPEN = 0, MLAU_BC1D_PERIODIC = 1 };
+/* Output file formats (mlau_sim_outdat). */
+enum { MLAU_OUT_F64 = 0, MLAU_OUT_F32_RANK = 1 };
 
 /* ---------------------------------------------------------------------- */
 /* 1. Drop-in drivers                                                      */
@@ -61,14 +63,17 @@ void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, do
                   int mpi_numx, int mpi_numy, int mpi_numz);
 
 /* Replaces the serial mhd_fd_ct_2d (2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-94,
- * caller 2D/SERIAL/OTvortex/main.cpp:30-31). */
+ * caller 2D/SERIAL/OTvortex/main.cpp:30-31).  The problem's boundary tables
+ * dnxs / dnys (periodic, Dirichlet or Neumann per array and axis) apply. */
 void mhd_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
                   double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
                   int xoff, int yoff, double gamma);
 
 /* Replaces the MPI form of mhd_fd_ct_2d (2D/MPI/OTvortex/mhd_fd_ct_2d.c:95-99,
- * caller 2D/MPI/OTvortex/main.cpp:48-50); C++ callers reach it under the
- * reference's overloaded name.  mpi_numx = mpi_numy = 1 required. */
+ * caller 2D/MPI/OTvortex/main.cpp:48-50; the same driver serves
+ * 2D/MPI/KHI with reflecting y walls); C++ callers reach it under the
+ * reference's overloaded name.  mpi_numx = mpi_numy = 1 required; each
+ * axis's table entries must be all zero or all nonzero. */
 void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
                       double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
                       int xoff, int yoff, double gamma, int mpi_rank, int mpi_numx,
@@ -94,6 +99,10 @@ void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, dou
  * calc_flr alternatives the headers ship; everything else follows ODR 2. */
 int mlau_set_scheme(int dim, int odr, int flux, int nrk);
 int mlau_set_bc_1d(int bc);
+/* The boundary tables the drop-in drivers see: the problem program's own
+ * dnxs / dnys / dnzs when it defines them (the library's weak all-zero
+ * tables give way to them at load time), else zeros. */
+int mlau_boundary_tables(int *dnx, int *dny, int *dnz);
 /* Arithmetic of the drop-in 3D driver: MLAU_FP64 (default; the reference's
  * arithmetic bit for bit) or MLAU_FP32_SPLIT. */
 int mlau_set_precision(int dim, int precision);
@@ -122,6 +131,13 @@ int mlau_sim_upload(mlau_sim *sim, const double *const *host8);
 int mlau_sim_download(mlau_sim *sim, double *const *host8);
 int mlau_sim_set_bx_1d(mlau_sim *sim, double bx);
 int mlau_sim_set_bc_1d(mlau_sim *sim, int bc);
+/* Boundary tables of a 2D FP64 simulation: dnx[8] / dny[8] as the problem's
+ * dnxs / dnys (2D/MPI/KHI/global.hpp:21-22; order ro mx my mz en bx by bz;
+ * 0 periodic, -1 Dirichlet, +1 Neumann mirror), each array's ghosts filled by
+ * its own entry as bc2d (2D/SERIAL/OTvortex/boundary.c:18-74), including the
+ * shock-sensor and cell-B fills inside the step.  All zero (the default) is
+ * periodic.  The drop-in 2D drivers apply the problem's own tables. */
+int mlau_sim_set_bc_2d(mlau_sim *sim, const int *dnx, const int *dny);
 /* nsteps full RK steps with fixed dt, enqueued on the simulation's stream. */
 int mlau_sim_step(mlau_sim *sim, double dt, int nsteps);
 /* CFL time step (3D/MPI/OTvortex/cflcheck.hpp:1-39, 2D cflcheck.hpp,
@@ -146,6 +162,33 @@ int mlau_sim_launches_per_step(mlau_sim *sim);
 /* Enqueue nsteps steps between two CUDA events recorded on the simulation's
  * stream and return the elapsed device time in milliseconds. */
 int mlau_sim_time_steps(mlau_sim *sim, double dt, int nsteps, double *ms);
+
+/* Checkpoint and output files in the reference's formats, written from and
+ * read into the device-resident state (2D/3D checkpoints; outputs in all
+ * dimensions), so runs restart across the reference and this library and the
+ * reference's readers take its output.
+ * Checkpoint - replaces bkup_save / bkup_load (3D/MPI/OTvortex/bkup.hpp:4-76,
+ * 2D/MPI/OTvortex/bkup.hpp): <dir>/bkup_stamp.dat ("%d %d\n" step, output count) and
+ * bkup_time.dat (3 doubles: time, dt, next output time) from rank 0, and
+ * bkup_data_%05d.dat (FP64 ro, mx, my, mz, bx, by, bz, en, ghosts included)
+ * per rank.  mlau_sim_bkup_load returns 1 and changes nothing when there is
+ * no stamp file (the reference's fresh start). */
+int mlau_sim_bkup_save(mlau_sim *sim, const char *dir, int n, int cnt, double tim, double dt,
+                       double trec, int rank);
+int mlau_sim_bkup_load(mlau_sim *sim, const char *dir, int *n, int *cnt, double *tim, double *dt,
+                       double *trec, int rank);
+/* Output - replaces the state part of dataio (3D/MPI/OTvortex/dataio.hpp:62-80,
+ * MLAU_OUT_F32_RANK: outdat_%05d_%05d.dat, FP32 ro mx my mz en bx by bz per
+ * rank; 2D/SERIAL/OTvortex/dataio.hpp:28-38, MLAU_OUT_F64: outdat_%05d.dat,
+ * FP64; in 1D the 1D driver's outdat_%05d.dat of ro mx my mz en by bz,
+ * 1D/SERIAL/shock/main.cpp:171-184).  FP32 conversion happens on the device. */
+int mlau_sim_outdat(mlau_sim *sim, const char *dir, int cnt, int rank, int format);
+/* The run's metadata as the same routines write them: first != 0 writes
+ * params.dat and offsets.dat (1D: params "bx gamma", xoff.dat) and starts
+ * t.dat; otherwise appends tim to t.dat.  Grid coordinate files are the
+ * problem's own and are not written. */
+int mlau_outdat_meta(const char *dir, int dim, int first, double tim, double gamma, double bx,
+                     int xoff, int yoff, int zoff);
 
 /* ---------------------------------------------------------------------- */
 /* 5. Batched 2D engine                                                    */

@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmlau_gb300.so")
 
 FLUX = {"mlau": 0, "lhlld": 1, "hlld": 2, "roe": 3}
 FP64, FP32_SPLIT = 0, 1
+OUT_F64, OUT_F32_RANK = 0, 1
 BC1D = {"open": 0, "periodic": 1}
 VARS = ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")
 KERNEL_KINDS = ("prim", "aux", "rec", "flux", "emf", "update", "copy", "cfl",
@@ -47,6 +48,7 @@ def _bind(lib):
     lib.mlau_sim_download.argtypes = [vp, C.POINTER(pd)]
     lib.mlau_sim_set_bx_1d.argtypes = [vp, d]
     lib.mlau_sim_set_bc_1d.argtypes = [vp, i]
+    lib.mlau_sim_set_bc_2d.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
     lib.mlau_sim_step.argtypes = [vp, d, i]
     lib.mlau_sim_cfl.argtypes = [vp, d, d, d, d, pd, pd]
     lib.mlau_sim_sync.argtypes = [vp]
@@ -63,6 +65,11 @@ def _bind(lib):
     lib.mlau_pin_host.argtypes = [vp, C.c_longlong]
     lib.mlau_unpin_host.argtypes = [vp]
     lib.mlau_set_device.argtypes = [i]
+    cp = C.c_char_p
+    lib.mlau_sim_bkup_save.argtypes = [vp, cp, i, i, d, d, d, i]
+    lib.mlau_sim_bkup_load.argtypes = [vp, cp, C.POINTER(i), C.POINTER(i), pd, pd, pd, i]
+    lib.mlau_sim_outdat.argtypes = [vp, cp, i, i, i]
+    lib.mlau_outdat_meta.argtypes = [cp, i, i, d, d, d, i, i, i]
     pi = C.POINTER(C.c_int)
     lib.mlau_batch_create.argtypes = [C.POINTER(vp), i, pi, pi, i, pd, pd, pd, pi, pd, pd, i]
     lib.mlau_batch_open.argtypes = [C.POINTER(vp), i, C.c_longlong, i, i, i]
@@ -201,6 +208,14 @@ def unpin(arr: np.ndarray):
     _check(lib().mlau_unpin_host(arr.ctypes.data))
 
 
+def outdat_meta(dir: str, dim: int, first: bool, tim: float, gamma: float, bx: float = 0.0,
+                xoff: int = 4, yoff: int = 4, zoff: int = 4):
+    """params.dat / offsets.dat (1D: xoff.dat) and t.dat as the reference's
+    output routines write them."""
+    _check(lib().mlau_outdat_meta(os.fsencode(dir), dim, int(first), tim, gamma, bx, xoff, yoff,
+                                  zoff))
+
+
 # --- device-resident handle ---------------------------------------------------
 class Sim:
     """A simulation resident on the GPU (handle API of include/mlau_gb300.h)."""
@@ -267,11 +282,38 @@ class Sim:
         _check(lib().mlau_sim_download(self._h, ptrs))
         return out
 
+    # --- the reference's checkpoint and output files ---
+    def bkup_save(self, dir: str, n: int, cnt: int, tim: float, dt: float, trec: float,
+                  rank: int = 0):
+        _check(lib().mlau_sim_bkup_save(self._h, os.fsencode(dir), n, cnt, tim, dt, trec, rank))
+
+    def bkup_load(self, dir: str, rank: int = 0):
+        """(n, cnt, tim, dt, trec) of the loaded checkpoint, or None when the
+        directory holds none."""
+        n, cnt = C.c_int(), C.c_int()
+        tim, dt, trec = C.c_double(), C.c_double(), C.c_double()
+        rc = lib().mlau_sim_bkup_load(self._h, os.fsencode(dir), C.byref(n), C.byref(cnt),
+                                      C.byref(tim), C.byref(dt), C.byref(trec), rank)
+        if rc == 1:
+            return None
+        _check(rc)
+        return n.value, cnt.value, tim.value, dt.value, trec.value
+
+    def outdat(self, dir: str, cnt: int, rank: int = 0, format: int = OUT_F64):
+        _check(lib().mlau_sim_outdat(self._h, os.fsencode(dir), cnt, rank, format))
+
     def set_bx(self, bx: float):
         _check(lib().mlau_sim_set_bx_1d(self._h, bx))
 
     def set_bc(self, bc: str):
         _check(lib().mlau_sim_set_bc_1d(self._h, BC1D[bc]))
+
+    def set_bc2d(self, dnx, dny):
+        """2D boundary tables (8 entries each, order ro mx my mz en bx by bz;
+        0 periodic, -1 Dirichlet, +1 Neumann)."""
+        tx = (C.c_int * 8)(*[int(v) for v in dnx])
+        ty = (C.c_int * 8)(*[int(v) for v in dny])
+        _check(lib().mlau_sim_set_bc_2d(self._h, tx, ty))
 
     def step(self, dt: float, nsteps: int = 1):
         _check(lib().mlau_sim_step(self._h, dt, nsteps))

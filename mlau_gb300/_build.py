@@ -38,6 +38,7 @@ UNITS = {
     "batch2d_split.cu": FAST32,
     "batch2d_plain.cu": EXACT,
     "batch1d_plain.cu": EXACT,
+    "dataio.cu": EXACT,
     "cxx_linkage.cpp": [],
 }
 

@@ -108,7 +108,7 @@ int launches_per_step(const Sim *s)
     // kernels per RK stage (device-to-device copies are not counted)
     if (s->precision == MLAU_FP32_SPLIT) return s->nrk * 7;
     if (s->g.dim == 3) return s->nrk * 10;
-    if (s->g.dim == 2) return s->nrk * 8;
+    if (s->g.dim == 2) return s->nrk * (s->walls2d ? 10 : 8);
     return s->nrk * 4 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
 }
 
@@ -178,6 +178,7 @@ int mlau_sim_destroy(mlau_sim *s)
     if (!s) return MLAU_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     s->timer.recs.clear();
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
     if (s->sp) split3d_free(s);
     for (void *p : s->allocs) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -210,10 +211,46 @@ int mlau_sim_download(mlau_sim *s, double *const *h)
     return s->sp ? split3d_check(s) : MLAU_OK;
 }
 
+// A captured step graph holds the scheme parameters of its capture.
+static void drop_graph(mlau_sim *s)
+{
+    if (s->gexec) {
+        cudaStreamSynchronize(s->stream);
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+}
+
 int mlau_sim_set_bx_1d(mlau_sim *s, double bx)
 {
     if (!s || s->g.dim != 1) { set_error("not a 1D simulation"); return MLAU_ERR_ARG; }
+    if (s->bx1d != bx) drop_graph(s);
     s->bx1d = bx;
+    return MLAU_OK;
+}
+
+int mlau_sim_set_bc_2d(mlau_sim *s, const int *dnx, const int *dny)
+{
+    if (!s || s->g.dim != 2 || s->precision != MLAU_FP64 || !dnx || !dny) {
+        set_error("boundary tables apply to 2D FP64 simulations");
+        return MLAU_ERR_ARG;
+    }
+    bool walls = false;
+    for (int v = 0; v < 8; v++) {
+        for (int t : {dnx[v], dny[v]})
+            if (t < -1 || t > 1) {
+                set_error("boundary table entries are -1, 0 or +1");
+                return MLAU_ERR_ARG;
+            }
+        walls = walls || dnx[v] != 0 || dny[v] != 0;
+    }
+    if (std::memcmp(s->bc2.x, dnx, sizeof(s->bc2.x)) || std::memcmp(s->bc2.y, dny, sizeof(s->bc2.y)))
+        drop_graph(s);
+    for (int v = 0; v < 8; v++) {
+        s->bc2.x[v] = dnx[v];
+        s->bc2.y[v] = dny[v];
+    }
+    s->walls2d = walls;
     return MLAU_OK;
 }
 
@@ -223,19 +260,69 @@ int mlau_sim_set_bc_1d(mlau_sim *s, int bc)
         set_error("bad 1D boundary request");
         return MLAU_ERR_ARG;
     }
+    if (s->bc1d != bc) drop_graph(s);
     s->bc1d = bc;
+    return MLAU_OK;
+}
+
+static int step_once(mlau_sim *s, double dt)
+{
+    if (s->precision == MLAU_FP32_SPLIT) return split3d_step(s, dt);
+    if (s->g.dim == 3) return plain3d_step(s, dt);
+    if (s->g.dim == 2) return plain2d_step(s, dt);
+    return plain1d_step(s, dt);
+}
+
+// Long runs at one dt replay a captured graph of kGraphSteps steps: one
+// launch per kGraphSteps steps instead of 4-10 per stage, which is what bounds
+// small problems.  The graph is rebuilt when dt changes; per-kernel timing
+// runs uncaptured.
+constexpr int kGraphSteps = 16;
+
+static int step_graph(mlau_sim *s, double dt)
+{
+    if (s->gexec && s->graph_dt == dt && s->graph_steps == kGraphSteps) return MLAU_OK;
+    if (s->gexec) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    MLAU_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = MLAU_OK;
+    for (int k = 0; k < kGraphSteps && rc == MLAU_OK; k++) rc = step_once(s, dt);
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (rc != MLAU_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) {
+        set_error("step graph capture: %s", cudaGetErrorString(e));
+        return MLAU_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        s->gexec = nullptr;
+        set_error("step graph instantiate: %s", cudaGetErrorString(ei));
+        return MLAU_ERR_CUDA;
+    }
+    s->graph_dt = dt;
+    s->graph_steps = kGraphSteps;
     return MLAU_OK;
 }
 
 int mlau_sim_step(mlau_sim *s, double dt, int nsteps)
 {
     if (!s || nsteps < 0 || !(dt == dt)) { set_error("bad step arguments"); return MLAU_ERR_ARG; }
-    for (int n = 0; n < nsteps; n++) {
-        int rc;
-        if (s->precision == MLAU_FP32_SPLIT) rc = split3d_step(s, dt);
-        else if (s->g.dim == 3) rc = plain3d_step(s, dt);
-        else if (s->g.dim == 2) rc = plain2d_step(s, dt);
-        else rc = plain1d_step(s, dt);
+    int n = 0;
+    if (nsteps >= kGraphSteps && !s->timer.on) {
+        int rc = step_graph(s, dt);
+        if (rc != MLAU_OK) return rc;
+        for (; n + kGraphSteps <= nsteps; n += kGraphSteps)
+            MLAU_CUDA(cudaGraphLaunch(s->gexec, s->stream));
+    }
+    for (; n < nsteps; n++) {
+        const int rc = step_once(s, dt);
         if (rc != MLAU_OK) return rc;
     }
     return MLAU_OK;
@@ -373,12 +460,15 @@ void init_scheme()
     g_scheme_init = true;
 }
 
-// Boundary tables of the problem program (3D/MPI/OTvortex/global.hpp:22-29).
-// Weak: a problem that defines them is checked; otherwise periodic is assumed.
+// Boundary tables of the problem program (3D/MPI/OTvortex/global.hpp:22-29,
+// 2D/MPI/KHI/global.hpp:21-22); weak zero definitions in cxx_linkage.cpp,
+// overridden by a problem program's own.  The references need default
+// visibility: this unit's host code is otherwise built with hidden extern
+// data, which would bind them to the library's own copies for good.
 extern "C" {
-__attribute__((weak)) extern int dnxs[8];
-__attribute__((weak)) extern int dnys[8];
-__attribute__((weak)) extern int dnzs[8];
+__attribute__((visibility("default"))) extern int dnxs[8];
+__attribute__((visibility("default"))) extern int dnys[8];
+__attribute__((visibility("default"))) extern int dnzs[8];
 }
 
 bool tables_periodic(int dim)
@@ -467,6 +557,16 @@ void mlau_release_dropin(void)
     }
 }
 
+int mlau_boundary_tables(int *dnx, int *dny, int *dnz)
+{
+    for (int v = 0; v < 8; v++) {
+        if (dnx) dnx[v] = dnxs[v];
+        if (dny) dny[v] = dnys[v];
+        if (dnz) dnz[v] = dnzs[v];
+    }
+    return MLAU_OK;
+}
+
 int mlau_set_bc_1d(int bc)
 {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -499,19 +599,39 @@ void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, do
     if (!c || run_dropin(c, h, dt) != MLAU_OK) report("mhd_fd_ct_3d");
 }
 
+// 2D drivers with the problem's dnxs/dnys.  The serial driver fills each
+// array's ghosts by its own table entry (bc2d); the MPI driver's single-rank
+// exchange decides periodicity per axis from entry 0 (mpi_sdrv2d,
+// 2D/MPI/OTvortex/boundary.c) - the two agree when each axis's entries are
+// all zero or all nonzero, which the MPI form therefore requires.
+static void dropin_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                      double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                      int xoff, int yoff, double gamma, bool mpi)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    static const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int *tx = dnxs ? dnxs : zero, *ty = dnys ? dnys : zero;
+    if (mpi)
+        for (const int *t : {tx, ty}) {
+            int nz = 0;
+            for (int v = 0; v < 8; v++) nz += t[v] != 0;
+            if (nz != 0 && nz != 8) {
+                set_error("MPI 2D driver: each axis's boundary entries must be all zero or all nonzero");
+                report("mhd_fd_ct_2d");
+                return;
+            }
+        }
+    mlau_sim *c = get_ctx(2, nx, ny, 1, xoff, yoff, 0, dx, dy, 1.0, gamma);
+    double *h[8] = {ro, mx, my, mz, en, bx, by, bz};
+    if (!c || mlau_sim_set_bc_2d(c, tx, ty) != MLAU_OK || run_dropin(c, h, dt) != MLAU_OK)
+        report("mhd_fd_ct_2d");
+}
+
 void mhd_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
                   double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
                   int xoff, int yoff, double gamma)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!tables_periodic(2)) {
-        set_error("only periodic boundaries (dnxs/dnys all 0) are implemented");
-        report("mhd_fd_ct_2d");
-        return;
-    }
-    mlau_sim *c = get_ctx(2, nx, ny, 1, xoff, yoff, 0, dx, dy, 1.0, gamma);
-    double *h[8] = {ro, mx, my, mz, en, bx, by, bz};
-    if (!c || run_dropin(c, h, dt) != MLAU_OK) report("mhd_fd_ct_2d");
+    dropin_2d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma, false);
 }
 
 void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
@@ -523,7 +643,7 @@ void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en
         report("mhd_fd_ct_2d");
         return;
     }
-    mhd_fd_ct_2d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma);
+    dropin_2d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma, true);
 }
 
 void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,

@@ -5,15 +5,10 @@
 // (2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-660) in the arithmetic of the 3D
 // FP32-split step (split3d.cu).
 #include "batch2d.cuh"
+#include "split_conv.cuh"
 
 namespace mlau {
 namespace {
-
-__device__ __forceinline__ float2 split2(double x)
-{
-    const float h = (float)x;
-    return make_float2(h, (float)(x - (double)h));
-}
 __device__ __forceinline__ float pf(float2 v) { return v.x + v.y; }
 __device__ __forceinline__ float pd(float2 u, float2 v) { return (u.x - v.x) + (u.y - v.y); }
 
@@ -58,22 +53,25 @@ __device__ void ph_prep(const BArgs &A, int nt, const BTile *tl, int rk)
         const double cy = face2cen(A.odr, by[w - I.nx], by[w], by[w + I.nx], by[w + 2 * I.nx]);
         const double bz = a.s[7][c];
         const double ro = a.s[0][c];
-        const float rof = (float)ro, irof = 1.f / rof;
-        const float vx = (float)a.s[1][c] * irof, vy = (float)a.s[2][c] * irof, vz = (float)a.s[3][c] * irof;
+        const float2 ro2 = split2(ro);
+        const float rof = ro2.x + ro2.y, irof = 1.f / rof;
+        const float vx = to_f32(a.s[1][c]) * irof, vy = to_f32(a.s[2][c]) * irof,
+                    vz = to_f32(a.s[3][c]) * irof;
         const float v2 = vx * vx + vy * vy + vz * vz;
         const double b2 = cx * cx + cy * cy + bz * bz;
-        const double pr = (I.gamma - 1.0) * (a.s[4][c] - 0.5 * ((double)(rof * v2) + b2));
-        a.q[0][c] = split2(ro);
+        const double pr = (I.gamma - 1.0) * (a.s[4][c] - 0.5 * (to_f64(rof * v2) + b2));
+        const float2 pr2 = split2(pr);
+        a.q[0][c] = ro2;
         a.q[1][c] = make_float2(vx, 0.f);
         a.q[2][c] = make_float2(vy, 0.f);
         a.q[3][c] = make_float2(vz, 0.f);
         a.q[4][c] = split2(cx);
         a.q[5][c] = split2(cy);
         a.q[6][c] = split2(bz);
-        a.q[7][c] = split2(pr);
-        a.bf[0][c] = (float)bx[c];
-        a.bf[1][c] = (float)by[c];
-        a.m2f[c] = v2 / ((float)I.gamma * (float)pr * irof);
+        a.q[7][c] = pr2;
+        a.bf[0][c] = to_f32(bx[c]);
+        a.bf[1][c] = to_f32(by[c]);
+        a.m2f[c] = v2 / (to_f32(I.gamma) * (pr2.x + pr2.y) * irof);
         if (rk == 0)
             for (int v = 0; v < 8; v++) a.u0[v][c] = a.s[v][c];
     });
@@ -241,14 +239,20 @@ __device__ void ph_update(const BArgs &A, int nt, const BTile *tl, int rk)
             const float *fx = a.Ff[0][cX[v]], *fy = a.Ff[1][cY[v]];
             const float div = dtdx * fdiff(A.odr, fx[c - 1], fx[c], fx[c + 1], fx[c + 2])
                               + dtdy * fdiff(A.odr, fy[c - nx], fy[c], fy[c + nx], fy[c + 2 * nx]);
-            out[sv[v]] = ra * a.u0[sv[v]][c] + rb * (a.s[sv[v]][c] - (double)div);
+            out[sv[v]] = ra * a.u0[sv[v]][c] + rb * (a.s[sv[v]][c] - to_f64(div));
         }
+        // CT curl in FP64 on the FP32 EMFs: the differences are exact; the
+        // stencil's 1/24 rides on dt/dx
         const float *ez = a.ezf;
-        const double ddx = I.dt / I.dx, ddy = I.dt / I.dy;
-        const double dy_ez = fdiff(A.odr, (double)ez[c - nx], (double)ez[c], (double)ez[c + nx],
-                                   (double)ez[c + 2 * nx]);
-        const double dx_ez = fdiff(A.odr, (double)ez[c - 1], (double)ez[c], (double)ez[c + 1],
-                                   (double)ez[c + 2]);
+        const bool o4 = lin_odr(A.odr) > 2;
+        const double c24 = o4 ? 1.0 / 24.0 : 1.0;
+        const double ddx = I.dt / I.dx * c24, ddy = I.dt / I.dy * c24;
+        auto d64 = [&](long long st) {
+            const double f0 = to_f64(ez[c - st]), f1 = to_f64(ez[c]), f2 = to_f64(ez[c + st]),
+                         f3 = to_f64(ez[c + 2 * st]);
+            return o4 ? 27.0 * (f2 - f1) - (f3 - f0) : f2 - f1;
+        };
+        const double dy_ez = d64(nx), dx_ez = d64(1);
         out[5] = ra * a.u0[5][c] + rb * (a.s[5][c] - ddy * dy_ez);
         out[6] = ra * a.u0[6][c] + rb * (a.s[6][c] + ddx * dx_ez);
         const int Nx = I.nx - 2 * I.off, Ny = I.ny - 2 * I.off;

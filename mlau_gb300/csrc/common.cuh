@@ -32,6 +32,25 @@ __host__ __device__ __forceinline__ int wrap_idx(int i, int n, int off)
     return (i < off) ? i + N : ((i >= n - off) ? i - N : i);
 }
 
+// Source of a possibly-ghost index along one axis under the reference's
+// boundary rule for one array (bc2d, 2D/SERIAL/OTvortex/boundary.c:18-74):
+// dn 0 periodic image; dn -1 (Dirichlet) / +1 (Neumann) mirror about the
+// boundary, multiplying *sgn by dn.  st 1 marks a face-centred array along
+// the axis: its right boundary face n-off is a computed value, not a ghost.
+__host__ __device__ __forceinline__ int bc_src(int i, int n, int off, int st, int dn, double *sgn)
+{
+    if (dn == 0) return wrap_idx(i, n, off);
+    if (i < off) { *sgn *= dn; return (2 * off - 1 + st) - i; }
+    if (i >= n - off + st) { *sgn *= dn; return (n - 2 * off + st) + (n - 1 - i); }
+    return i;
+}
+
+// Boundary tables of a 2D problem (the problem's dnxs/dnys, variable order
+// ro mx my mz en bx by bz); all zero = periodic.
+struct Bc2 {
+    int x[8], y[8];
+};
+
 // Kernel-kind identifiers for the optional per-kernel event timing.
 enum KernelKind {
     KK_PRIM = 0, KK_AUX, KK_REC, KK_FLUX, KK_EMF, KK_UPDATE, KK_COPY, KK_CFL,

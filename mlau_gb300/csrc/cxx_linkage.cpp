@@ -55,3 +55,15 @@ void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, dou
 {
     mlau_c_fd4c_1d(ro, mx, my, mz, en, by, bz, bx, dt, dx, nx, xoff, gamma);
 }
+
+// Boundary tables of the problem program (3D/MPI/OTvortex/global.hpp:22-29,
+// 2D/MPI/KHI/global.hpp:21-22; order ro mx my mz en bx by bz, 0 periodic).
+// Defined here, all zero, as weak symbols with default visibility: a problem
+// program that defines its own tables (every reference problem does, in
+// global.hpp) overrides these when it is loaded - the linker exports an
+// executable's definition of a symbol that a linked library also defines.
+extern "C" {
+__attribute__((weak, visibility("default"))) int dnxs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+__attribute__((weak, visibility("default"))) int dnys[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+__attribute__((weak, visibility("default"))) int dnzs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+}

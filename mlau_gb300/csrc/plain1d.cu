@@ -11,10 +11,15 @@
 namespace mlau {
 namespace {
 
-__global__ void k_prim1(PlainFields f, int nx, double bx, double gamma)
+// Primitives; at the first stage also the copy of the state U^n (seven small
+// copies would cost more than the kernel).
+__global__ void k_prim1(PlainFields f, int nx, double bx, double gamma, int save_u0)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
+    if (save_u0)
+        for (int v = 0; v < 8; v++)
+            if (v != 5) f.u0[v][i] = f.s[v][i];
     const double ro = f.s[0][i], iro = 1.0 / ro;
     const double vx = f.s[1][i] * iro, vy = f.s[2][i] * iro, vz = f.s[3][i] * iro;
     const double by = f.s[6][i], bz = f.s[7][i];
@@ -77,14 +82,17 @@ __global__ void k_flux1(PlainFields f, int nx, int which, double bx, double gamm
     for (int n = 0; n < 7; n++) f.F[0][n][i] = F[n];
 }
 
-// openbc1d_mhd (1D/SERIAL/shock/openbc1d_mhd.c:21-175); one thread, both sides.
+// openbc1d_mhd (1D/SERIAL/shock/openbc1d_mhd.c:21-175).  The two sides read
+// and write disjoint cells (interior width >= ghost depth), so each runs in
+// its own block: block 0 the left side, block 1 the right.
 __global__ void k_openbc1(PlainFields f, int nx, int xoff, double bx, double dtdx, double gamma)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (threadIdx.x != 0 || blockIdx.x > 1) return;
     double *ro = f.s[0], *mx = f.s[1], *my = f.s[2], *mz = f.s[3], *en = f.s[4], *by = f.s[6],
            *bz = f.s[7];
     const double bx2 = bx * bx;
-    for (int side = 0; side <= 1; side++) {
+    {
+        const int side = blockIdx.x;
         const int sgn = side ? -1 : 1;
         const int si = side ? (nx - xoff - 1) : xoff;
         const int so = si - sgn;
@@ -188,21 +196,13 @@ int plain1d_step(Sim *s, double dt)
     cudaStream_t st = s->stream;
     const int nx = g.nx, off = g.ox;
     const double dtdx = dt / g.dx;
-    {
-        TimedLaunch tl(&s->timer, KK_COPY);
-        for (int v = 0; v < 8; v++) {
-            if (v == 5) continue;
-            MLAU_CUDA(cudaMemcpyAsync(f.u0[v], f.s[v], sizeof(double) * g.n,
-                                      cudaMemcpyDeviceToDevice, st));
-        }
-    }
     const int T = 128;
     for (int rk = 0; rk < s->nrk; rk++) {
         double ra, rb;
         rk_coef(s->nrk, rk, ra, rb);
         {
             TimedLaunch tl(&s->timer, KK_PRIM);
-            k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, s->bx1d, s->gamma);
+            k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, s->bx1d, s->gamma, rk == 0);
         }
         {
             TimedLaunch tl(&s->timer, KK_REC);
@@ -214,7 +214,7 @@ int plain1d_step(Sim *s, double dt)
         }
         if (s->bc1d == MLAU_BC1D_OPEN && rk == 0) {
             TimedLaunch tl(&s->timer, KK_AUX);
-            k_openbc1<<<1, 1, 0, st>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
+            k_openbc1<<<2, 1, 0, st>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
         }
         {
             TimedLaunch tl(&s->timer, KK_UPDATE);
@@ -237,19 +237,14 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
                     double bx, double dt, double dx, double gamma, cudaStream_t st)
 {
     const double dtdx = dt / dx;
-    for (int v = 0; v < 8; v++) {
-        if (v == 5) continue;
-        MLAU_CUDA(cudaMemcpyAsync(f.u0[v], f.s[v], sizeof(double) * nx, cudaMemcpyDeviceToDevice,
-                                  st));
-    }
     const int T = 128;
     for (int rk = 0; rk < nrk; rk++) {
         double ra, rb;
         rk_coef(nrk, rk, ra, rb);
-        k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma);
+        k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma, rk == 0);
         k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, odr, bx, gamma);
         k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
-        if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<1, 1, 0, st>>>(f, nx, off, bx, dtdx, gamma);
+        if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<2, 1, 0, st>>>(f, nx, off, bx, dtdx, gamma);
         k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(f, nx, off, odr, ra, rb, dtdx,
                                                             bc == MLAU_BC1D_PERIODIC);
         MLAU_CUDA(cudaGetLastError());

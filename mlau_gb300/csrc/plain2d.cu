@@ -1,22 +1,33 @@
-// Plain FP64 2D step: one SSP-RK step of ideal MHD with constrained transport
-// on a periodic plane, the GPU form of 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-660.
+// Plain FP64 2D step: one SSP-RK step of ideal MHD with constrained transport,
+// the GPU form of 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-660, with the problem's
+// boundary tables (periodic, or Dirichlet / Neumann mirrors per array and
+// axis as bc2d, 2D/SERIAL/OTvortex/boundary.c:18-74).
 // Bz is cell-centred and advanced with the fluxes; Bx, By live on faces and
 // are advanced by the curl of the corner EMF Ez.  Compiled with --fmad=false
 // so the arithmetic is the reference's, bit for bit.
+#include <algorithm>
+
 #include "stencil.cuh"
 
 namespace mlau {
 namespace {
 
-__global__ void __launch_bounds__(TPB) k_prim2(PlainFields f, Dims d, Box b, int odr, double gamma)
+// Cell-centred B: computed at the cell itself or, in the ghost frame, at its
+// boundary source times the table's sign (calc_bc then bc2d with dnxs[5..6],
+// :186-200).
+__global__ void __launch_bounds__(TPB)
+k_prim2(PlainFields f, Dims d, Box b, int odr, double gamma, Bc2 bc)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
     const long long sy = d.nx;
-    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), 0);
+    double gx = 1.0, gy = 1.0;
+    const int ix = bc_src(i, d.nx, d.ox, 0, bc.x[5], &gx), jx = bc_src(j, d.ny, d.oy, 0, bc.y[5], &gx);
+    const int iy = bc_src(i, d.nx, d.ox, 0, bc.x[6], &gy), jy = bc_src(j, d.ny, d.oy, 0, bc.y[6], &gy);
+    const long long wx = d.at(ix, jx, 0), wy = d.at(iy, jy, 0);
     const double *bx = f.s[5], *by = f.s[6];
-    const double cx = face2cen(odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
-    const double cy = face2cen(odr, by[w - sy], by[w], by[w + sy], by[w + 2 * sy]);
+    const double cx = gx * face2cen(odr, bx[wx - 1], bx[wx], bx[wx + 1], bx[wx + 2]);
+    const double cy = gy * face2cen(odr, by[wy - sy], by[wy], by[wy + sy], by[wy + 2 * sy]);
     const long long s = d.at(i, j, 0);
     const double ro = f.s[0][s];
     const double iro = 1.0 / ro;
@@ -34,7 +45,9 @@ __global__ void __launch_bounds__(TPB) k_prim2(PlainFields f, Dims d, Box b, int
     f.cy[s] = cy;
 }
 
-__global__ void __launch_bounds__(TPB) k_aux2(PlainFields f, Dims d, Box b)
+// Shock sensors, with the sign rules of their ghost fill (:262-271): dvx
+// takes -dnxs[1] along x and +dnys[1] along y, dvy +dnxs[2] and -dnys[2].
+__global__ void __launch_bounds__(TPB) k_aux2(PlainFields f, Dims d, Box b, Bc2 bc)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
@@ -42,9 +55,12 @@ __global__ void __launch_bounds__(TPB) k_aux2(PlainFields f, Dims d, Box b)
     const long long s = d.at(i, j, 0);
     f.ct[0][s] = (i >= 1 && j >= 1) ? ct_weight(f.vx, f.vy, f.s[0], f.s[5], f.s[6], s, sy, 1, sy, 1)
                                     : 0.5;
-    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), 0);
-    f.dv[0][s] = vmin((f.vx[w + 1] - f.vx[w]), (f.vx[w] - f.vx[w - 1]));
-    f.dv[1][s] = vmin((f.vy[w + sy] - f.vy[w]), (f.vy[w] - f.vy[w - sy]));
+    double g0 = 1.0, g1 = 1.0;
+    const int i0 = bc_src(i, d.nx, d.ox, 0, -bc.x[1], &g0), j0 = bc_src(j, d.ny, d.oy, 0, bc.y[1], &g0);
+    const int i1 = bc_src(i, d.nx, d.ox, 0, bc.x[2], &g1), j1 = bc_src(j, d.ny, d.oy, 0, -bc.y[2], &g1);
+    const long long w0 = d.at(i0, j0, 0), w1 = d.at(i1, j1, 0);
+    f.dv[0][s] = g0 * vmin((f.vx[w0 + 1] - f.vx[w0]), (f.vx[w0] - f.vx[w0 - 1]));
+    f.dv[1][s] = g1 * vmin((f.vy[w1 + sy] - f.vy[w1]), (f.vy[w1] - f.vy[w1 - sy]));
 }
 
 // Sweep along x (D=0): (vn, vt, vu) = (vx, vy, vz), (bt, bu) = (cy, bz), the
@@ -137,8 +153,11 @@ __global__ void __launch_bounds__(TPB) k_emf2(PlainFields f, Dims d, Box b, int 
     f.e[2][c] = ez;
 }
 
+// RK combine + CT curl of the interior.  With periodic tables each cell also
+// writes its periodic images; otherwise k_face2 and k_bc2 follow.
 __global__ void __launch_bounds__(TPB)
-k_update2(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dtdx, double dtdy)
+k_update2(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dtdx, double dtdy,
+          int images)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
@@ -164,6 +183,11 @@ k_update2(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dt
         const double dd = fdiff(odr, ez[s - 1], ez[s], ez[s + 1], ez[s + 2]);
         out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] + dtdx * dd);
     }
+    if (!images) {
+#pragma unroll
+        for (int v = 0; v < 8; v++) f.s[v][s] = out[v];
+        return;
+    }
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy;
     int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
     int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -175,6 +199,48 @@ k_update2(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dt
 #pragma unroll
             for (int v = 0; v < 8; v++) f.s[v][t] = out[v];
         }
+    }
+}
+
+// The right boundary faces the CT loops also update (:593-632 run one face
+// further, i < nx-xoff+1 for Bx and j < ny-yoff+1 for By); they survive the
+// boundary fill only where that axis mirrors the face array.
+__global__ void __launch_bounds__(TPB)
+k_face2(PlainFields f, Dims d, int odr, double ra, double rb, double dtdx, double dtdy, int do_x,
+        int do_y)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long sy = d.nx;
+    const double *ez = f.e[2];
+    const int ny_in = d.ny - 2 * d.oy, nx_in = d.nx - 2 * d.ox;
+    if (do_x && t < ny_in) {  // Bx at i = nx - xoff
+        const long long s = d.at(d.nx - d.ox, d.oy + t, 0);
+        const double dd = fdiff(odr, ez[s - sy], ez[s], ez[s + sy], ez[s + 2 * sy]);
+        f.s[5][s] = ra * f.u0[5][s] + rb * (f.s[5][s] - dtdy * dd);
+    }
+    if (do_y && t < nx_in) {  // By at j = ny - yoff
+        const long long s = d.at(d.ox + t, d.ny - d.oy, 0);
+        const double dd = fdiff(odr, ez[s - 1], ez[s], ez[s + 1], ez[s + 2]);
+        f.s[6][s] = ra * f.u0[6][s] + rb * (f.s[6][s] + dtdx * dd);
+    }
+}
+
+// Ghost fill of the conserved arrays with the tables (:636-638): each ghost
+// takes its boundary source (periodic image or mirror, composed over the two
+// axes) times the signs.  Sources are interior cells or computed faces.
+__global__ void __launch_bounds__(TPB) k_bc2(PlainFields f, Dims d, Box b, Bc2 bc)
+{
+    int i, j, k;
+    if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+    if (i >= d.ox && i < d.nx - d.ox && j >= d.oy && j < d.ny - d.oy) return;
+    const long long s = d.at(i, j, 0);
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+        double g = 1.0;
+        const int si = bc_src(i, d.nx, d.ox, v == 5, bc.x[v], &g);
+        const int sj = bc_src(j, d.ny, d.oy, v == 6, bc.y[v], &g);
+        if (si == i && sj == j) continue;
+        f.s[v][s] = g * f.s[v][d.at(si, sj, 0)];
     }
 }
 
@@ -217,11 +283,12 @@ int plain2d_step(Sim *s, double dt)
         rk_coef(s->nrk, rk, ra, rb);
         {
             TimedLaunch tl(&s->timer, KK_PRIM);
-            k_prim2<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->odr, s->gamma);
+            k_prim2<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->odr, s->gamma,
+                                                                  s->bc2);
         }
         {
             TimedLaunch tl(&s->timer, KK_AUX);
-            k_aux2<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all);
+            k_aux2<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->bc2);
         }
         for (int D = 0; D < 2; D++) {
             const View2 v = make_view2(f, D);
@@ -247,7 +314,13 @@ int plain2d_step(Sim *s, double dt)
         {
             TimedLaunch tl(&s->timer, KK_UPDATE);
             k_update2<<<blocks_for(inner.count(), TPB), TPB, 0, st>>>(f, d, inner, s->odr, ra, rb,
-                                                                      dtdx, dtdy);
+                                                                      dtdx, dtdy, !s->walls2d);
+            if (s->walls2d) {
+                const int n = std::max(g.nx, g.ny);
+                k_face2<<<blocks_for(n, TPB), TPB, 0, st>>>(f, d, s->odr, ra, rb, dtdx, dtdy,
+                                                            s->bc2.x[5] != 0, s->bc2.y[6] != 0);
+                k_bc2<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->bc2);
+            }
         }
         MLAU_CUDA(cudaGetLastError());
     }

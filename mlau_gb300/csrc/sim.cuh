@@ -34,6 +34,8 @@ struct Sim {
     int odr, flux, nrk, precision;
     int bc1d = MLAU_BC1D_OPEN;
     double bx1d = 0.0;
+    Bc2 bc2{};           // 2D boundary tables (all zero: periodic)
+    bool walls2d = false;  // some 2D table entry is not periodic
     cudaStream_t stream = nullptr;
     PlainFields f{};
     SplitFields *sp = nullptr;
@@ -42,6 +44,10 @@ struct Sim {
     double *d_red = nullptr;   // device scratch for reductions (2 doubles)
     int *d_flag = nullptr;     // device status flag
     KernelTimer timer;
+    // steps replayed from a captured CUDA graph (small problems are launch bound)
+    cudaGraphExec_t gexec = nullptr;
+    double graph_dt = 0.0;
+    int graph_steps = 0;
 };
 
 int plain3d_alloc(Sim *s);

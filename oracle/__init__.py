@@ -42,6 +42,11 @@ class Port:
             lib.oracle_fd_ct_3d.restype = None
             lib.oracle_fd_ct_2d.argtypes = [_dp] * 8 + [d, d, d] + [i] * 4 + [d, i, i, i]
             lib.oracle_fd_ct_2d.restype = None
+            pi8 = C.POINTER(C.c_int)
+            lib.oracle_fd_ct_2d_bc.argtypes = [_dp] * 8 + [d, d, d] + [i] * 4 + [d, i, i, i, pi8, pi8]
+            lib.oracle_fd_ct_2d_bc.restype = None
+            lib.oracle_bc2d_state.argtypes = [_dp] * 8 + [i] * 4 + [pi8, pi8]
+            lib.oracle_bc2d_state.restype = None
             lib.oracle_fd4c_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d, i, i, i, i]
             lib.oracle_fd4c_1d.restype = None
             lib.oracle_cfl_3d.argtypes = [_cdp] * 8 + [i] * 6 + [d, d, d, d, d, C.POINTER(d)]
@@ -64,10 +69,24 @@ class Port:
                                   _flux_id(flux), nrk)
 
     @classmethod
-    def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3):
+    def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3, dnx=None,
+               dny=None):
+        """dnx/dny: the problem's boundary tables (8 ints, order ro mx my mz en
+        bx by bz; 0 periodic, -1 Dirichlet, +1 Neumann); None is periodic."""
         ny, nx = s["ro"].shape
-        cls.lib().oracle_fd_ct_2d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
-                                  dt, dx, dy, nx, ny, off, off, gamma, odr, _flux_id(flux), nrk)
+        tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
+        cls.lib().oracle_fd_ct_2d_bc(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                     dt, dx, dy, nx, ny, off, off, gamma, odr, _flux_id(flux), nrk,
+                                     tab(dnx), tab(dny))
+
+    @classmethod
+    def setbc2d(cls, s, dnx, dny, off=4):
+        """Apply the boundary tables to a 2D state's ghost cells in place (the
+        reference problems' setbc after initialisation)."""
+        ny, nx = s["ro"].shape
+        tab = lambda t: (C.c_int * 8)(*[int(x) for x in t])
+        cls.lib().oracle_bc2d_state(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                    nx, ny, off, off, tab(dnx), tab(dny))
 
     @classmethod
     def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open"):
@@ -139,11 +158,24 @@ class Ref:
             dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma)
 
     @classmethod
-    def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3):
+    def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3, dnx=None,
+               dny=None):
+        """dnx/dny: boundary tables written into the build's dnxs/dnys
+        globals (global.hpp) for this call; None is periodic."""
         ny, nx = s["ro"].shape
-        cls._get(2, odr, _flux_id(flux), nrk).ref_step(
-            *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
-            dt, dx, dy, 1.0, nx, ny, 1, off, off, 0, gamma)
+        lib = cls._get(2, odr, _flux_id(flux), nrk)
+        gx = (C.c_int * 8).in_dll(lib, "dnxs")
+        gy = (C.c_int * 8).in_dll(lib, "dnys")
+        for g, t in ((gx, dnx), (gy, dny)):
+            for v in range(8):
+                g[v] = 0 if t is None else int(t[v])
+        try:
+            lib.ref_step(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                         dt, dx, dy, 1.0, nx, ny, 1, off, off, 0, gamma)
+        finally:
+            for g in (gx, gy):
+                for v in range(8):
+                    g[v] = 0
 
     @classmethod
     def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open"):

@@ -122,6 +122,25 @@ def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
     return out
 
 
+def build_ref_io() -> str:
+    """Compile the reference's checkpoint and output routines
+    (3D/MPI/OTvortex/bkup.hpp, 3D/MPI/OTvortex/dataio.hpp,
+    2D/SERIAL/OTvortex/dataio.hpp) into oracle/_ref/libref_io.so through
+    oracle/ref_io_harness.cpp; return its path."""
+    if not reference_available():
+        raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
+    out = os.path.join(REF_OUT, "libref_io.so")
+    src = os.path.join(HERE, "ref_io_harness.cpp")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out
+    os.makedirs(REF_OUT, exist_ok=True)
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O1", "-fPIC", "-shared", "-w", "-I" + REF_ROOT, "-o", tmp, src]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+    os.replace(tmp, out)
+    return out
+
+
 def all_variants():
     for dim in (3, 2):
         for odr in (1, 2, 3, 4):

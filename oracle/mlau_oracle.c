@@ -69,19 +69,41 @@ static void fill3d(double *f, int nx, int ny, int nz, int xoff, int yoff, int zo
             }
 }
 
-/* bc2d periodic branch, 2D/SERIAL/OTvortex/boundary.c:28-57. */
-static void fill2d(double *f, int nx, int ny, int xoff, int yoff)
+/* bc2d, 2D/SERIAL/OTvortex/boundary.c:18-74: one array, X then Y; dn 0 is
+   periodic, -1 Dirichlet (antisymmetric mirror), +1 Neumann (mirror); st 1
+   marks a face-centred array along that axis (its right boundary face is
+   computed by the update, not filled). */
+static void bc2d_o(double *f, int nx, int ny, int xoff, int yoff, int stx, int dnx, int sty,
+                   int dny)
 {
-    for (int j = 0; j < ny; j++)
-        for (int i = 0; i < xoff; i++) {
-            f[(long)nx * j + (nx - 1 - i)] = f[(long)nx * j + (2 * xoff - 1 - i)];
-            f[(long)nx * j + i] = f[(long)nx * j + (nx - 2 * xoff + i)];
+    if (dnx == 0) {
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < xoff; i++) {
+                f[(long)nx * j + (nx - 1 - i)] = f[(long)nx * j + (2 * xoff - 1 - i)];
+                f[(long)nx * j + i] = f[(long)nx * j + (nx - 2 * xoff + i)];
+            }
+    } else {
+        for (int j = 0; j < ny; j++) {
+            for (int i = 0; i < xoff; i++)
+                f[(long)nx * j + i] = dnx * f[(long)nx * j + (2 * xoff - 1 + stx) - i];
+            for (int i = 0; i < xoff - stx; i++)
+                f[(long)nx * j + (nx - 1 - i)] = dnx * f[(long)nx * j + (nx - 2 * xoff + stx) + i];
         }
-    for (int j = 0; j < yoff; j++)
-        for (int i = 0; i < nx; i++) {
-            f[(long)nx * (ny - 1 - j) + i] = f[(long)nx * (2 * yoff - 1 - j) + i];
-            f[(long)nx * j + i] = f[(long)nx * (ny - 2 * yoff + j) + i];
-        }
+    }
+    if (dny == 0) {
+        for (int j = 0; j < yoff; j++)
+            for (int i = 0; i < nx; i++) {
+                f[(long)nx * (ny - 1 - j) + i] = f[(long)nx * (2 * yoff - 1 - j) + i];
+                f[(long)nx * j + i] = f[(long)nx * (ny - 2 * yoff + j) + i];
+            }
+    } else {
+        for (int j = 0; j < yoff; j++)
+            for (int i = 0; i < nx; i++)
+                f[(long)nx * j + i] = dny * f[(long)nx * ((2 * yoff - 1 + sty) - j) + i];
+        for (int j = 0; j < yoff - sty; j++)
+            for (int i = 0; i < nx; i++)
+                f[(long)nx * (ny - 1 - j) + i] = dny * f[(long)nx * ((ny - 2 * yoff + sty) + j) + i];
+    }
 }
 
 /*
@@ -460,12 +482,36 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
 }
 
 /* ------------------------------------------------------------------------ */
-/* 2D driver: 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-660, periodic.            */
+/* 2D driver: 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c:91-660; boundary tables     */
+/* dnx/dny as the problem's dnxs/dnys (global.hpp), NULL = periodic.        */
 /* ------------------------------------------------------------------------ */
 void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
                      double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
                      int xoff, int yoff, double gamma, int odr, int flx, int nrk)
 {
+    oracle_fd_ct_2d_bc(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma,
+                       odr, flx, nrk, NULL, NULL);
+}
+
+/* The problems' setbc (2D/SERIAL/OTvortex/setbc.hpp:1-6): bc2d on the eight
+   conserved arrays with the boundary tables. */
+void oracle_bc2d_state(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                       double *by, double *bz, int nx, int ny, int xoff, int yoff,
+                       const int *dnx, const int *dny)
+{
+    static const int stx[8] = {0, 0, 0, 0, 0, 1, 0, 0}, sty[8] = {0, 0, 0, 0, 0, 0, 1, 0};
+    double *p[8] = {ro, mx, my, mz, en, bx, by, bz};
+    for (int v = 0; v < 8; v++) bc2d_o(p[v], nx, ny, xoff, yoff, stx[v], dnx[v], sty[v], dny[v]);
+}
+
+void oracle_fd_ct_2d_bc(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                        double *by, double *bz, double dt, double dx, double dy, int nx, int ny,
+                        int xoff, int yoff, double gamma, int odr, int flx, int nrk,
+                        const int *dnx_in, const int *dny_in)
+{
+    static const int zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    static const int stx[8] = {0, 0, 0, 0, 0, 1, 0, 0}, sty[8] = {0, 0, 0, 0, 0, 0, 1, 0};
+    const int *dnx = dnx_in ? dnx_in : zero8, *dny = dny_in ? dny_in : zero8;
     const long n = (long)nx * ny;
     const double dtdx = dt / dx, dtdy = dt / dy;
     double *state[8] = {ro, mx, my, mz, bx, by, bz, en};
@@ -495,8 +541,8 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
                 long s = (long)nx * j + i;
                 cy[s] = o_face2cen(odr, by[s - sy], by[s], by[s + sy], by[s + 2 * sy]);
             }
-        fill2d(cx, nx, ny, xoff, yoff);
-        fill2d(cy, nx, ny, xoff, yoff);
+        bc2d_o(cx, nx, ny, xoff, yoff, 0, dnx[5], 0, dny[5]);
+        bc2d_o(cy, nx, ny, xoff, yoff, 0, dnx[6], 0, dny[6]);
         /* primitives (:203-223) */
 #pragma omp parallel for
         for (long s = 0; s < n; s++) {
@@ -536,8 +582,8 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
                 dvx[s] = o_min((vx[s + 1] - vx[s]), (vx[s] - vx[s - 1]));
                 dvy[s] = o_min((vy[s + sy] - vy[s]), (vy[s] - vy[s - sy]));
             }
-        fill2d(dvx, nx, ny, xoff, yoff);
-        fill2d(dvy, nx, ny, xoff, yoff);
+        bc2d_o(dvx, nx, ny, xoff, yoff, 0, -dnx[1], 0, +dny[1]);
+        bc2d_o(dvy, nx, ny, xoff, yoff, 0, +dnx[2], 0, -dny[2]);
 
         /* X faces (:273-362): (vn,vt,vu)=(vx,vy,vz), (bt,bu)=(cy,bz); only the
          * By flux is split.  Y faces (:404-493): (vy,vz,vx), (bz,cx); only Bx. */
@@ -602,7 +648,9 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en,
                 double d = o_diff(odr, ez[s - 1], ez[s], ez[s + 1], ez[s + 2]);
                 by[s] = ra * u0[5 * n + s] + rb * (by[s] + dtdx * d);
             }
-        for (int v = 0; v < 8; v++) fill2d(state[v], nx, ny, xoff, yoff);
+        /* boundary of the 8 conserved arrays (:636-638), in the reference's order */
+        double *p[8] = {ro, mx, my, mz, en, bx, by, bz};
+        for (int v = 0; v < 8; v++) bc2d_o(p[v], nx, ny, xoff, yoff, stx[v], dnx[v], sty[v], dny[v]);
     }
     free(u0);
     double *tmp[] = {vx, vy, vz, pr, cx, cy, m2, ez, ctw, dvx, dvy, fcx, fcy};

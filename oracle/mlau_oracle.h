@@ -44,6 +44,19 @@ void oracle_fd_ct_2d(double *ro, double *mx, double *my, double *mz,
                      double dt, double dx, double dy,
                      int nx, int ny, int xoff, int yoff,
                      double gamma, int odr, int flux, int nrk);
+/* The problems' setbc: the boundary tables applied to the conserved arrays. */
+void oracle_bc2d_state(double *ro, double *mx, double *my, double *mz,
+                       double *en, double *bx, double *by, double *bz,
+                       int nx, int ny, int xoff, int yoff, const int *dnx, const int *dny);
+/* Same with the problem's boundary tables dnx[8]/dny[8] (global.hpp dnxs /
+ * dnys, variable order ro mx my mz en bx by bz; 0 periodic, -1 Dirichlet,
+ * +1 Neumann); NULL tables are periodic. */
+void oracle_fd_ct_2d_bc(double *ro, double *mx, double *my, double *mz,
+                        double *en, double *bx, double *by, double *bz,
+                        double dt, double dx, double dy,
+                        int nx, int ny, int xoff, int yoff,
+                        double gamma, int odr, int flux, int nrk,
+                        const int *dnx, const int *dny);
 
 /* One full SSP-RK step of 1D MHD (7 variables, constant bx), in place.
  * Restates 1D/SERIAL/shock/mhd_fd4c_1d.c:60-271 (bc=OPEN, open boundary at

@@ -53,6 +53,16 @@ CASES_1D = [  # (name, n, odr, flux, bc, seed)
     ("1d_mlau_o5_open", 64, 5, "mlau", "open", 6),
     ("1d_lhlld_o6_periodic", 64, 6, "lhlld", "periodic", 7),
 ]
+# 2D with non-periodic boundary tables (the problem's dnxs / dnys), whole
+# arrays stored: (name, n, odr, flux, seed, dnx, dny); the initial ghosts are
+# filled with the tables first, as the problems' setbc does
+KHI = ((0, 0, 0, 0, 0, 0, 0, 0), (1, 1, -1, 1, 1, 1, -1, 1))  # 2D/MPI/KHI/global.hpp:21-22
+CASES_2D_WALLS = [
+    ("2d_lhlld_o4_khi", 16, 4, "lhlld", 11, *KHI),
+    ("2d_mlau_o5_khi", 16, 5, "mlau", 12, *KHI),
+    ("2d_hlld_o2_walls", 16, 2, "hlld", 13, (1, -1, 1, 1, 1, -1, 1, 1), (1, 1, -1, 1, 1, 1, -1, 1)),
+    ("2d_roe_o4_neumann", 16, 4, "roe", 14, (1,) * 8, (1,) * 8),
+]
 STEPS = (1, 4)
 
 
@@ -96,6 +106,26 @@ def main(only=()):
             done = nstep
             for k, v in s.items():
                 out[f"out{nstep}_" + k] = interior(v, 2)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, n, odr, flux, seed, dnx, dny in CASES_2D_WALLS:
+        if skip(name):
+            continue
+        from oracle import Port
+        st, m = ics.turbulence_2d(n=n, ny=n - 4, seed=seed, odr=odr, vrms=0.4)
+        Port.setbc2d(st, dnx, dny)
+        dt = 0.3 * m["dx"] / m["vfast"]
+        out = {"dt": dt, "dx": m["dx"], "dy": m["dy"], "gamma": m["gamma"], "odr": odr,
+               "flux": flux, "dnx": np.array(dnx), "dny": np.array(dny)}
+        for k, v in st.items():
+            out["in_" + k] = v.copy()
+        s = ics.copy_state(st)
+        done = 0
+        for nstep in STEPS:
+            for _ in range(nstep - done):
+                Ref.step2d(s, dt, m["dx"], m["dy"], odr=odr, flux=flux, dnx=dnx, dny=dny)
+            done = nstep
+            for k, v in s.items():
+                out[f"out{nstep}_" + k] = v.copy()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     for name, n, odr, flux, bc, seed in CASES_1D:
         if skip(name):

@@ -7,6 +7,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -76,3 +77,20 @@ def test_loading_fails_loudly_without_library(tmp_path, monkeypatch):
     monkeypatch.setattr(M, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(M.MlauError):
         M.lib()
+
+
+def test_problem_boundary_tables_reach_the_library(tmp_path):
+    """A program that defines dnxs / dnys (as every reference problem's
+    global.hpp does) overrides the library's weak all-zero tables."""
+    import mlau_gb300
+    import subprocess
+    src = os.path.join(os.path.dirname(__file__), "c", "tables_probe.c")
+    exe = tmp_path / "tables_probe"
+    libdir = os.path.dirname(mlau_gb300.LIB_PATH)
+    subprocess.run(["gcc", "-O1", src, "-o", str(exe), f"-L{libdir}", "-lmlau_gb300",
+                    f"-Wl,-rpath,{libdir}"], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    got = np.array([int(v) for v in out]).reshape(8, 3)
+    assert list(got[:, 0]) == [0] * 8
+    assert list(got[:, 1]) == [1, 1, -1, 1, 1, 1, -1, 1]
+    assert list(got[:, 2]) == [0] * 8

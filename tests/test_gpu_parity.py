@@ -20,11 +20,14 @@ FLUXES = ("mlau", "lhlld", "hlld", "roe")
 def gpu_run(dim, st, steps, dt, **kw):
     bx = kw.pop("bx", None)
     bc = kw.pop("bc", None)
+    tables = kw.pop("tables", None)
     with M.Sim(dim, st["ro"].shape, **kw) as s:
         if bx is not None:
             s.set_bx(bx)
         if bc is not None:
             s.set_bc(bc)
+        if tables is not None:
+            s.set_bc2d(*tables)
         s.upload(st)
         s.step(dt, steps)
         return s.download()
@@ -44,8 +47,9 @@ def test_golden_3d(name):
 def test_golden_2d(name):
     prm, s, outs = load_golden(name)
     for n, ref in outs.items():
-        got = gpu_run(2, s, n, prm["dt"], dx=prm["dx"], dy=prm["dx"], gamma=prm["gamma"],
-                      odr=prm["odr"], flux=prm["flux"])
+        tables = (prm["dnx"], prm["dny"]) if "dnx" in prm else None
+        got = gpu_run(2, s, n, prm["dt"], dx=prm["dx"], dy=prm.get("dy", prm["dx"]),
+                      gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"], tables=tables)
         assert equal_values(got, ref), f"{name} after {n} steps: {max_rel_diff(got, ref)}"
 
 

@@ -28,8 +28,8 @@ def test_port_matches_golden_2d(port, name):
     done = 0
     for n in sorted(outs):
         for _ in range(n - done):
-            port.step2d(s, prm["dt"], prm["dx"], prm["dx"], gamma=prm["gamma"], odr=prm["odr"],
-                        flux=prm["flux"])
+            port.step2d(s, prm["dt"], prm["dx"], prm.get("dy", prm["dx"]), gamma=prm["gamma"],
+                        odr=prm["odr"], flux=prm["flux"], dnx=prm.get("dnx"), dny=prm.get("dny"))
         done = n
         assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
 
