@@ -47,6 +47,10 @@ class Port:
             lib.oracle_fd_ct_2d_bc.restype = None
             lib.oracle_bc2d_state.argtypes = [_dp] * 8 + [i] * 4 + [pi8, pi8]
             lib.oracle_bc2d_state.restype = None
+            lib.oracle_diff_ctfield_e.argtypes = [_dp] * 4 + [d, d, d, d, i, i, i, i, d, i, i, pi8, pi8]
+            lib.oracle_diff_ctfield_e.restype = None
+            lib.oracle_ns_viscous_2d.argtypes = [_cdp] + [_dp] * 4 + [d, d, d, d, i, i, i, i, d, i, i, pi8, pi8]
+            lib.oracle_ns_viscous_2d.restype = None
             lib.oracle_fd4c_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d, i, i, i, i]
             lib.oracle_fd4c_1d.restype = None
             lib.oracle_cfl_3d.argtypes = [_cdp] * 8 + [i] * 6 + [d, d, d, d, d, C.POINTER(d)]
@@ -78,6 +82,22 @@ class Port:
         cls.lib().oracle_fd_ct_2d_bc(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
                                      dt, dx, dy, nx, ny, off, off, gamma, odr, _flux_id(flux), nrk,
                                      tab(dnx), tab(dny))
+
+    @classmethod
+    def resistive2d(cls, s, eta0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None, dny=None):
+        """diff_ctfield_e of the MRX driver file, in place on en, bx, by, bz."""
+        ny, nx = s["ro"].shape
+        tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
+        cls.lib().oracle_diff_ctfield_e(s["en"], s["bx"], s["by"], s["bz"], eta0, dt, dx, dy, nx,
+                                        ny, off, off, gamma, odr, nrk, tab(dnx), tab(dny))
+
+    @classmethod
+    def viscous2d(cls, s, nu0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None, dny=None):
+        """ns_viscous_2d of the MRX driver file, in place on mx, my, mz, en."""
+        ny, nx = s["ro"].shape
+        tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
+        cls.lib().oracle_ns_viscous_2d(s["ro"], s["mx"], s["my"], s["mz"], s["en"], nu0, dt, dx,
+                                       dy, nx, ny, off, off, gamma, odr, nrk, tab(dnx), tab(dny))
 
     @classmethod
     def setbc2d(cls, s, dnx, dny, off=4):
@@ -182,3 +202,62 @@ class Ref:
         nx = s["ro"].shape[0]
         cls._get(1, odr, _flux_id(flux), nrk, bc).ref_step_1d(
             *[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")], bx, dt, dx, nx, off, gamma)
+
+
+class RefMRX:
+    """ctypes binding of the reference's 2D MRX driver file (hyperbolic step
+    with the MC limiter at ODR 2, resistive and viscous operators) built into
+    oracle/_ref; boundary tables written into the build's dnxs/dnys."""
+
+    _libs: dict = {}
+
+    @classmethod
+    def _get(cls, odr, nrk):
+        key = (odr, nrk)
+        if key not in cls._libs:
+            lib = C.CDLL(build.build_ref_mrx(odr, nrk))
+            d, i = C.c_double, C.c_int
+            lib.ref_mrx_step.argtypes = [_dp] * 8 + [d, d, d, i, i, i, i, d]
+            lib.ref_diff_ctfield_e.argtypes = [_dp] * 4 + [d, d, d, d, i, i, i, i, d]
+            lib.ref_ns_viscous_2d.argtypes = [_dp] * 5 + [d, d, d, d, i, i, i, i, d]
+            for f in (lib.ref_mrx_step, lib.ref_diff_ctfield_e, lib.ref_ns_viscous_2d):
+                f.restype = None
+            cls._libs[key] = lib
+        return cls._libs[key]
+
+    @classmethod
+    def _tables(cls, lib, dnx, dny):
+        for name, t in (("dnxs", dnx), ("dnys", dny)):
+            g = (C.c_int * 8).in_dll(lib, name)
+            for v in range(8):
+                g[v] = 0 if t is None else int(t[v])
+
+    @classmethod
+    def _call(cls, fn, lib, dnx, dny, *args):
+        cls._tables(lib, dnx, dny)
+        try:
+            fn(*args)
+        finally:
+            cls._tables(lib, None, None)
+
+    @classmethod
+    def step(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None, dny=None):
+        ny, nx = s["ro"].shape
+        lib = cls._get(odr, nrk)
+        cls._call(lib.ref_mrx_step, lib, dnx, dny,
+                  *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                  dt, dx, dy, nx, ny, off, off, gamma)
+
+    @classmethod
+    def resistive2d(cls, s, eta0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None, dny=None):
+        ny, nx = s["ro"].shape
+        lib = cls._get(odr, nrk)
+        cls._call(lib.ref_diff_ctfield_e, lib, dnx, dny, s["en"], s["bx"], s["by"], s["bz"], eta0,
+                  dt, dx, dy, nx, ny, off, off, gamma)
+
+    @classmethod
+    def viscous2d(cls, s, nu0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None, dny=None):
+        ny, nx = s["ro"].shape
+        lib = cls._get(odr, nrk)
+        cls._call(lib.ref_ns_viscous_2d, lib, dnx, dny, s["ro"], s["mx"], s["my"], s["mz"], s["en"],
+                  nu0, dt, dx, dy, nx, ny, off, off, gamma)

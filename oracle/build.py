@@ -141,6 +141,39 @@ def build_ref_io() -> str:
     return out
 
 
+def build_ref_mrx(odr: int = 2, nrk: int = 3) -> str:
+    """Compile the reference's 2D MRX driver file (hyperbolic step with the MC
+    limiter, resistive and viscous operators; 2D/MPI/MRX/mhd_fd_ct_2d.c with its
+    ODR / R_K lines set) and 2D/MPI/MRX/boundary.c with the single-rank mpi.h
+    stub and oracle/ref_mrx_harness.cpp; return the .so path."""
+    if not reference_available():
+        raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
+    name = f"ref_mrx_o{odr}_rk{nrk}"
+    out = os.path.join(REF_OUT, f"lib{name}.so")
+    harness = os.path.join(HERE, "ref_mrx_harness.cpp")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(harness):
+        return out
+    d = os.path.join(REF_ROOT, "2D/MPI/MRX")
+    with open(os.path.join(d, "mhd_fd_ct_2d.c")) as fh:
+        text = fh.read()
+    text, n1 = re.subn(r"^#define ODR \(\d\)", f"#define ODR ({odr})", text, count=1, flags=re.M)
+    text, n2 = re.subn(r"^#define R_K \(\d\)", f"#define R_K ({nrk})", text, count=1, flags=re.M)
+    if (n1, n2) != (1, 1):
+        raise RuntimeError("reference MRX driver layout not recognised; patch failed")
+    src_dir = os.path.join(REF_OUT, "src", name)
+    os.makedirs(src_dir, exist_ok=True)
+    drv = os.path.join(src_dir, "mhd_fd_ct_2d.cpp")
+    with open(drv, "w") as fh:
+        fh.write(text)
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["g++", "-x", "c++", *CFLAGS, "-I" + os.path.join(REF_ROOT, "include"),
+           "-I" + os.path.join(HERE, "ref_stub"), "-o", tmp, drv, os.path.join(d, "boundary.c"),
+           harness, "-lm"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+    os.replace(tmp, out)
+    return out
+
+
 def all_variants():
     for dim in (3, 2):
         for odr in (1, 2, 3, 4):

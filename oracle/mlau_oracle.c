@@ -907,3 +907,241 @@ void oracle_reconst(int full, int odr, const double *prim35, double bn, double g
         for (int m = 0; m < 5; m++) q[k][m] = prim35[5 * k + m];
     o_reconst(full, odr, q, bn, gamma, ul, ur);
 }
+
+/* ------------------------------------------------------------------------ */
+/* 2D MRX operators: 2D/MPI/MRX/mhd_fd_ct_2d.c:726-1174, one rank.           */
+/* ------------------------------------------------------------------------ */
+
+/* Ghost fill of arrays p[0..nn) by the MPI 2D drivers' single-rank boundary
+   routines (2D/MPI/MRX/boundary.c): mpi_sdrv2d - periodic along an axis whose
+   table entry 0 is zero, X then Y, every array - then per array mpi_xbc2d and
+   mpi_ybc2d, mirroring where the array's own entry is nonzero. */
+static void o_bc2d_mpi(double **p, int nn, const int *stx, const int *sty, const int *dnx,
+                       const int *dny, int dnx0, int dny0, int nx, int ny, int xoff, int yoff)
+{
+    if (dnx0 == 0)
+        for (int n = 0; n < nn; n++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < xoff; i++) {
+                    p[n][(long)nx * j + (nx - 1 - i)] = p[n][(long)nx * j + (2 * xoff - 1 - i)];
+                    p[n][(long)nx * j + i] = p[n][(long)nx * j + (nx - 2 * xoff + i)];
+                }
+    if (dny0 == 0)
+        for (int n = 0; n < nn; n++)
+            for (int j = 0; j < yoff; j++)
+                for (int i = 0; i < nx; i++) {
+                    p[n][(long)nx * (ny - 1 - j) + i] = p[n][(long)nx * (2 * yoff - 1 - j) + i];
+                    p[n][(long)nx * j + i] = p[n][(long)nx * (ny - 2 * yoff + j) + i];
+                }
+    for (int n = 0; n < nn; n++) {
+        double *f = p[n];
+        if (dnx[n] != 0) {
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < xoff; i++)
+                    f[(long)nx * j + i] = dnx[n] * f[(long)nx * j + (2 * xoff - 1 + stx[n]) - i];
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < xoff - stx[n]; i++)
+                    f[(long)nx * j + (nx - 1 - i)] =
+                        dnx[n] * f[(long)nx * j + (nx - 2 * xoff + stx[n]) + i];
+        }
+        if (dny[n] != 0) {
+            for (int j = 0; j < yoff; j++)
+                for (int i = 0; i < nx; i++)
+                    f[(long)nx * j + i] = dny[n] * f[(long)nx * ((2 * yoff - 1 + sty[n]) - j) + i];
+            for (int j = 0; j < yoff - sty[n]; j++)
+                for (int i = 0; i < nx; i++)
+                    f[(long)nx * (ny - 1 - j) + i] =
+                        dny[n] * f[(long)nx * ((ny - 2 * yoff + sty[n]) + j) + i];
+        }
+    }
+}
+
+static const int o_zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
+/* diff_ctfield_e (2D/MPI/MRX/mhd_fd_ct_2d.c:726-950): resistive diffusion of
+   the CT field with uniform resistivity eta0, energy updated by the
+   resistive Poynting flux. */
+void oracle_diff_ctfield_e(double *en, double *bx, double *by, double *bz, double eta0,
+                           double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                           double gamma, int odr, int nrk, const int *dnx_in, const int *dny_in)
+{
+    (void)gamma;
+    const int *dnx = dnx_in ? dnx_in : o_zero8, *dny = dny_in ? dny_in : o_zero8;
+    static const int stx[8] = {0, 0, 0, 0, 0, 1, 0, 0}, sty[8] = {0, 0, 0, 0, 0, 0, 1, 0};
+    const long n = (long)nx * ny;
+    const double dtdx = dt / dx, dtdy = dt / dy, idx = 1. / dx, idy = 1. / dy;
+    double *ut = alloc_d(4 * n), *fx = alloc_d(n), *fy = alloc_d(n);
+    double *ex = alloc_d(n), *ey = alloc_d(n), *ez = alloc_d(n);
+    memcpy(ut, bx, sizeof(double) * n);
+    memcpy(ut + n, by, sizeof(double) * n);
+    memcpy(ut + 2 * n, bz, sizeof(double) * n);
+    memcpy(ut + 3 * n, en, sizeof(double) * n);
+#define S2(i, j) ((long)nx * (j) + (i))
+    for (int rk = 0; rk < nrk; rk++) {
+        double ra, rb;
+        rk_coef(nrk, rk, &ra, &rb);
+        /* resistive E = eta0 * J (:772-801) */
+        for (int j = 2; j < ny - 1; j++)
+            for (int i = 2; i < nx - 1; i++) {
+                const long s = S2(i, j);
+                double jx = +o_diff(odr, bz[S2(i, j - 2)], bz[S2(i, j - 1)], bz[S2(i, j)], bz[S2(i, j + 1)]) * idy;
+                double jy = -o_diff(odr, bz[S2(i - 2, j)], bz[S2(i - 1, j)], bz[S2(i, j)], bz[S2(i + 1, j)]) * idx;
+                double jz = +o_diff(odr, by[S2(i - 2, j)], by[S2(i - 1, j)], by[S2(i, j)], by[S2(i + 1, j)]) * idx
+                            - o_diff(odr, bx[S2(i, j - 2)], bx[S2(i, j - 1)], bx[S2(i, j)], bx[S2(i, j + 1)]) * idy;
+                ex[s] = eta0 * jx;
+                ey[s] = eta0 * jy;
+                ez[s] = eta0 * jz;
+            }
+        /* energy flux along X (:802-826) */
+        for (int j = 2; j < ny - 2; j++)
+            for (int i = 2; i < nx - 1; i++) {
+                const long s = S2(i, j);
+                double ep = ey[s];
+                double bp = o_face2cen(odr, bz[S2(i - 2, j)], bz[S2(i - 1, j)], bz[S2(i, j)], bz[S2(i + 1, j)]);
+                double em = 0.5 * (ez[s] + ez[S2(i, j + 1)]);
+                double bm = 0.5 * (o_face2cen(odr, by[S2(i - 2, j)], by[S2(i - 1, j)], by[S2(i, j)], by[S2(i + 1, j)])
+                                   + o_face2cen(odr, by[S2(i - 2, j + 1)], by[S2(i - 1, j + 1)], by[S2(i, j + 1)], by[S2(i + 1, j + 1)]));
+                fx[s] = ep * bp - em * bm;
+            }
+        /* energy flux along Y (:827-852) */
+        for (int j = 2; j < ny - 1; j++)
+            for (int i = 2; i < nx - 2; i++) {
+                const long s = S2(i, j);
+                double ep = 0.5 * (ez[s] + ez[S2(i + 1, j)]);
+                double bp = 0.5 * (o_face2cen(odr, bx[S2(i, j - 2)], bx[S2(i, j - 1)], bx[S2(i, j)], bx[S2(i, j + 1)])
+                                   + o_face2cen(odr, bx[S2(i + 1, j - 2)], bx[S2(i + 1, j - 1)], bx[S2(i + 1, j)], bx[S2(i + 1, j + 1)]));
+                double em = ex[s];
+                double bm = o_face2cen(odr, bz[S2(i, j - 2)], bz[S2(i, j - 1)], bz[S2(i, j)], bz[S2(i, j + 1)]);
+                fy[s] = ep * bp - em * bm;
+            }
+        /* CT Bx, By (:854-889) */
+        for (int j = yoff; j < ny - yoff; j++)
+            for (int i = xoff; i < nx - xoff + 1; i++) {
+                const long s = S2(i, j);
+                double du = o_diff(odr, ez[S2(i, j - 1)], ez[s], ez[S2(i, j + 1)], ez[S2(i, j + 2)]);
+                bx[s] = ra * ut[s] + rb * (bx[s] - dtdy * du);
+            }
+        for (int j = yoff; j < ny - yoff + 1; j++)
+            for (int i = xoff; i < nx - xoff; i++) {
+                const long s = S2(i, j);
+                double du = o_diff(odr, ez[S2(i - 1, j)], ez[s], ez[S2(i + 1, j)], ez[S2(i + 2, j)]);
+                by[s] = ra * ut[n + s] + rb * (by[s] + dtdx * du);
+            }
+        /* Bz and energy (:890-921) */
+        for (int j = yoff; j < ny - yoff; j++)
+            for (int i = xoff; i < nx - xoff; i++) {
+                const long s = S2(i, j);
+                double d00 = o_diff(odr, ey[S2(i - 1, j)], ey[s], ey[S2(i + 1, j)], ey[S2(i + 2, j)]);
+                double d01 = o_diff(odr, fx[S2(i - 1, j)], fx[s], fx[S2(i + 1, j)], fx[S2(i + 2, j)]);
+                double d10 = o_diff(odr, ex[S2(i, j - 1)], ex[s], ex[S2(i, j + 1)], ex[S2(i, j + 2)]);
+                double d11 = o_diff(odr, fy[S2(i, j - 1)], fy[s], fy[S2(i, j + 1)], fy[S2(i, j + 2)]);
+                bz[s] = ra * ut[2 * n + s] + rb * (bz[s] - dtdx * d00 + dtdy * d10);
+                en[s] = ra * ut[3 * n + s] + rb * (en[s] - dtdx * d01 - dtdy * d11);
+            }
+        double *p[3] = {bx, by, bz};
+        o_bc2d_mpi(p, 3, stx + 5, sty + 5, dnx + 5, dny + 5, dnx[0], dny[0], nx, ny, xoff, yoff);
+    }
+    o_bc2d_mpi(&en, 1, stx + 4, sty + 4, dnx + 4, dny + 4, dnx[0], dny[0], nx, ny, xoff, yoff);
+    free(ut); free(fx); free(fy); free(ex); free(ey); free(ez);
+}
+
+/* ns_viscous_2d (2D/MPI/MRX/mhd_fd_ct_2d.c:952-1174): viscous term of the 2D
+   Navier-Stokes equation with uniform kinematic viscosity nu0. */
+void oracle_ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, double *en,
+                          double nu0, double dt, double dx, double dy, int nx, int ny, int xoff,
+                          int yoff, double gamma, int odr, int nrk, const int *dnx_in,
+                          const int *dny_in)
+{
+    (void)gamma;
+    const int *dnx = dnx_in ? dnx_in : o_zero8, *dny = dny_in ? dny_in : o_zero8;
+    static const int st0[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const long n = (long)nx * ny;
+    const double idx = 1. / dx, idy = 1. / dy, dtdx = dt * idx, dtdy = dt * idy;
+    const double c2 = 2. / 3., c4 = 4. / 3.;
+    double *ir = alloc_d(n), *ut = alloc_d(4 * n), *fx = alloc_d(4 * n), *fy = alloc_d(4 * n);
+    for (long s = 0; s < n; s++) {
+        ir[s] = 1.0 / ro[s];
+        mx[s] *= ir[s];
+        my[s] *= ir[s];
+        mz[s] *= ir[s];
+        ut[s] = mx[s];
+        ut[n + s] = my[s];
+        ut[2 * n + s] = mz[s];
+        ut[3 * n + s] = en[s];
+    }
+    for (int rk = 0; rk < nrk; rk++) {
+        double ra, rb;
+        rk_coef(nrk, rk, &ra, &rb);
+        /* flux along X (:999-1043) */
+        for (int j = 1; j < ny - 1; j++)
+            for (int i = 2; i < nx - 1; i++) {
+                const long s = S2(i, j);
+                double ro0 = 0.5 * (ro[S2(i, j)] + ro[S2(i - 1, j)]);
+                double rnu = ro0 * nu0;
+                double vx0 = o_face2cen(odr, mx[S2(i - 2, j)], mx[S2(i - 1, j)], mx[s], mx[S2(i + 1, j)]);
+                double vy0 = o_face2cen(odr, my[S2(i - 2, j)], my[S2(i - 1, j)], my[s], my[S2(i + 1, j)]);
+                double vz0 = o_face2cen(odr, mz[S2(i - 2, j)], mz[S2(i - 1, j)], mz[s], mz[S2(i + 1, j)]);
+                double dvxdx = o_diff(odr, mx[S2(i - 2, j)], mx[S2(i - 1, j)], mx[s], mx[S2(i + 1, j)]) * idx;
+                double dvydx = o_diff(odr, my[S2(i - 2, j)], my[S2(i - 1, j)], my[s], my[S2(i + 1, j)]) * idx;
+                double dvzdx = o_diff(odr, mz[S2(i - 2, j)], mz[S2(i - 1, j)], mz[s], mz[S2(i + 1, j)]) * idx;
+                double dv[4];
+                for (int m = 0; m < 4; m++)
+                    dv[m] = 0.5 * (mx[S2(i - 2 + m, j + 1)] - mx[S2(i - 2 + m, j - 1)]);
+                double dvxdy = o_face2cen(odr, dv[0], dv[1], dv[2], dv[3]) * idy;
+                for (int m = 0; m < 4; m++)
+                    dv[m] = 0.5 * (my[S2(i - 2 + m, j + 1)] - my[S2(i - 2 + m, j - 1)]);
+                double dvydy = o_face2cen(odr, dv[0], dv[1], dv[2], dv[3]) * idy;
+                fx[s] = -rnu * (c4 * dvxdx - c2 * dvydy);
+                fx[n + s] = -rnu * (dvydx + dvxdy);
+                fx[2 * n + s] = -rnu * (dvzdx);
+                fx[3 * n + s] = fx[s] * vx0 + fx[n + s] * vy0 + fx[2 * n + s] * vz0;
+            }
+        /* flux along Y (:1045-1089) */
+        for (int j = 2; j < ny - 1; j++)
+            for (int i = 1; i < nx - 1; i++) {
+                const long s = S2(i, j);
+                double ro0 = 0.5 * (ro[S2(i, j)] + ro[S2(i, j - 1)]);
+                double rnu = ro0 * nu0;
+                double vx0 = o_face2cen(odr, mx[S2(i, j - 2)], mx[S2(i, j - 1)], mx[s], mx[S2(i, j + 1)]);
+                double vy0 = o_face2cen(odr, my[S2(i, j - 2)], my[S2(i, j - 1)], my[s], my[S2(i, j + 1)]);
+                double vz0 = o_face2cen(odr, mz[S2(i, j - 2)], mz[S2(i, j - 1)], mz[s], mz[S2(i, j + 1)]);
+                double dvxdy = o_diff(odr, mx[S2(i, j - 2)], mx[S2(i, j - 1)], mx[s], mx[S2(i, j + 1)]) * idy;
+                double dvydy = o_diff(odr, my[S2(i, j - 2)], my[S2(i, j - 1)], my[s], my[S2(i, j + 1)]) * idy;
+                double dvzdy = o_diff(odr, mz[S2(i, j - 2)], mz[S2(i, j - 1)], mz[s], mz[S2(i, j + 1)]) * idy;
+                double dv[4];
+                for (int m = 0; m < 4; m++)
+                    dv[m] = 0.5 * (mx[S2(i + 1, j - 2 + m)] - mx[S2(i - 1, j - 2 + m)]);
+                double dvxdx = o_face2cen(odr, dv[0], dv[1], dv[2], dv[3]) * idx;
+                for (int m = 0; m < 4; m++)
+                    dv[m] = 0.5 * (my[S2(i + 1, j - 2 + m)] - my[S2(i - 1, j - 2 + m)]);
+                double dvydx = o_face2cen(odr, dv[0], dv[1], dv[2], dv[3]) * idx;
+                fy[s] = -rnu * (dvxdy + dvydx);
+                fy[n + s] = -rnu * (c4 * dvydy - c2 * dvxdx);
+                fy[2 * n + s] = -rnu * (dvzdy);
+                fy[3 * n + s] = fy[s] * vx0 + fy[n + s] * vy0 + fy[2 * n + s] * vz0;
+            }
+        /* update (:1091-1139) */
+        double *vel[3] = {mx, my, mz};
+        for (int j = yoff; j < ny - yoff; j++)
+            for (int i = xoff; i < nx - xoff; i++) {
+                const long s = S2(i, j);
+                double du[2][4];
+                for (int c = 0; c < 4; c++) {
+                    du[0][c] = o_diff(odr, fx[c * n + S2(i - 1, j)], fx[c * n + s], fx[c * n + S2(i + 1, j)], fx[c * n + S2(i + 2, j)]);
+                    du[1][c] = o_diff(odr, fy[c * n + S2(i, j - 1)], fy[c * n + s], fy[c * n + S2(i, j + 1)], fy[c * n + S2(i, j + 2)]);
+                }
+                for (int c = 0; c < 3; c++)
+                    vel[c][s] = ra * ut[c * n + s] + rb * (vel[c][s] - (dtdx * du[0][c] + dtdy * du[1][c]) * ir[s]);
+                en[s] = ra * ut[3 * n + s] + rb * (en[s] - (dtdx * du[0][3] + dtdy * du[1][3]));
+            }
+        o_bc2d_mpi(vel, 3, st0, st0, dnx + 1, dny + 1, dnx[0], dny[0], nx, ny, xoff, yoff);
+    }
+    o_bc2d_mpi(&en, 1, st0, st0, dnx + 4, dny + 4, dnx[0], dny[0], nx, ny, xoff, yoff);
+    for (long s = 0; s < n; s++) {
+        mx[s] *= ro[s];
+        my[s] *= ro[s];
+        mz[s] *= ro[s];
+    }
+    free(ir); free(ut); free(fx); free(fy);
+}
+#undef S2

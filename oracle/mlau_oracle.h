@@ -96,4 +96,17 @@ void oracle_reconst(int full, int odr, const double *prim35, double bn, double g
 #ifdef __cplusplus
 }
 #endif
+/* 2D MRX operators (2D/MPI/MRX/mhd_fd_ct_2d.c:726-1174) for one rank:
+ * resistive diffusion of the CT field (uniform eta0, energy updated by the
+ * resistive Poynting flux) and the viscous term (uniform kinematic nu0).
+ * odr/nrk as the driver file's ODR / R_K; dnx/dny the problem's dnxs/dnys
+ * (NULL: periodic), with the MPI drivers' single-rank boundary routines. */
+void oracle_diff_ctfield_e(double *en, double *bx, double *by, double *bz, double eta0,
+                           double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                           double gamma, int odr, int nrk, const int *dnx, const int *dny);
+void oracle_ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, double *en,
+                          double nu0, double dt, double dx, double dy, int nx, int ny, int xoff,
+                          int yoff, double gamma, int odr, int nrk, const int *dnx,
+                          const int *dny);
+
 #endif

@@ -4,6 +4,7 @@
  * copy.  TEST INFRASTRUCTURE ONLY. */
 #ifndef ORACLE_MPI_STUB_H
 #define ORACLE_MPI_STUB_H
+#include <stdio.h>
 #include <string.h>
 typedef int MPI_Comm;
 typedef int MPI_Datatype;
@@ -15,6 +16,7 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_INT 4
 #define MPI_MAX 1
 #define MPI_SUM 2
+#define MPI_MIN 3
 static inline int MPI_Init(int *a, char ***b) { (void)a; (void)b; return 0; }
 static inline int MPI_Finalize(void) { return 0; }
 static inline int MPI_Comm_rank(MPI_Comm c, int *r) { (void)c; *r = 0; return 0; }
