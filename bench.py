@@ -377,6 +377,75 @@ def run_step2d(args):
                              "kind": "port", "sample": f"{n}^2 x {args.cpu_steps} steps"}}
 
 
+def run_mrx2d(args):
+    """The MRX problem's main loop (2D/MPI/MRX/main.cpp:48-68) at its size,
+    2048 x 256 cells: hyperbolic step (MC-limited MUSCL, LHLLD, CT, RK3),
+    resistive diffusion of B with its energy flux, viscosity, and the CFL dt
+    read back every loop, as the reference does.  FP64 plain (bit-exact);
+    the CPU restatement of the same loop timed beside it."""
+    import mlau_gb300 as M
+    from mlau_gb300 import ics
+    st, m = ics.mrx_2d(seed=1)
+    ny, nx = st["ro"].shape
+    cells = (nx - 8) * (ny - 8)
+
+    def loop(s, dt, n):
+        for _ in range(n):
+            s.step(dt, 1)
+            s.resistive(m["eta0"], dt)
+            s.viscous(m["nu0"], dt)
+            dt, _ = s.cfl(m["cfl"], m["dr"], m["vfast"], dt)
+        return dt
+
+    with M.Sim(2, st["ro"].shape, dx=m["dx"], dy=m["dy"], gamma=m["gamma"], odr=5,
+               flux="lhlld", nrk=3) as s:
+        s.set_bc2d(*m["tables"])
+        s.upload(st)
+        dt = loop(s, m["dt"], args.warmup)
+        s.sync()
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            dt = loop(s, dt, args.steps)
+            s.sync()
+            sec = time.perf_counter() - t0
+        # the operators alone, CUDA-event timed on the library's stream
+        s.set_timing(False)
+        op_ms = {}
+        for op, coef in (("resistive", m["eta0"]), ("viscous", m["nu0"])):
+            fn = getattr(s, op)
+            for _ in range(3):
+                fn(coef, dt)
+            s.sync()
+            t1 = time.perf_counter()
+            for _ in range(args.steps):
+                fn(coef, dt)
+            s.sync()
+            op_ms[op] = (time.perf_counter() - t1) * 1e3 / args.steps
+        launches = (s.launches_per_step + 3 * 4 + 1 + 3 * 3 + 3 + 1) * args.steps
+    v = cells * args.steps / sec
+    from oracle import Port
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    cst = ics.copy_state(st)
+    kw = dict(gamma=m["gamma"], odr=5, nrk=3, dnx=m["tables"][0], dny=m["tables"][1])
+    t0 = time.perf_counter()
+    for _ in range(args.cpu_steps):
+        Port.step2d(cst, m["dt"], m["dx"], m["dy"], flux="lhlld", **kw)
+        Port.resistive2d(cst, m["eta0"], m["dt"], m["dx"], m["dy"], **kw)
+        Port.viscous2d(cst, m["nu0"], m["dt"], m["dx"], m["dy"], **kw)
+    cv = cells * args.cpu_steps / (time.perf_counter() - t0)
+    return {"metric": "MRX loop zone-updates/s (step + resistive + viscous + CFL)", "value": v,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (Harris sheet with seeded Vy noise; the reference seeds from the clock)",
+            "config": {"workload": "MRX 2048 x 256, x periodic / y walls, MUSCL-MC + LHLLD + CT + "
+                                   "RK3, eta0 = nu0 = 2e-3, CFL 0.2 dt read back per loop",
+                       "l2": "state 8 x 4.3 MB fits in L2: steady-state throughput, no flush"},
+            "operator_ms": op_ms, "gpu_launches": launches, "clocks": clk.summary(),
+            "cpu_baseline": {"value": cv, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port", "sample": f"MRX 2048 x 256 x {args.cpu_steps} loops"}}
+
+
 def run_step1d(args):
     """Config C0: 1D Riemann problem, 2048 cells, MLAU + MUSCL (minmod) + RK3,
     gamma=2, CFL 0.4, open boundaries, dt fixed from the initial state, run to
@@ -521,7 +590,8 @@ def main():
     ap.add_argument("--mach", type=float, default=1e-2)
     ap.add_argument("--precision", choices=("both", "fp64", "split"), default="both",
                     help="both: FP32-split is the headline value, FP64 beside it")
-    ap.add_argument("--workload", choices=("step3d", "step2d", "step1d", "batch2d", "serve"),
+    ap.add_argument("--workload", choices=("step3d", "step2d", "step1d", "batch2d", "serve",
+                                           "mrx2d"),
                     default="step3d")
     ap.add_argument("--n2d", type=int, default=512)
     ap.add_argument("--cpu-steps", type=int, default=2)
@@ -546,6 +616,10 @@ def main():
             if R.rank == 0:
                 fn = run_step2d if args.workload == "step2d" else run_step1d
                 print(json.dumps(fn(args)), flush=True)
+            return
+        if args.workload == "mrx2d":
+            if R.rank == 0:
+                print(json.dumps(run_mrx2d(args)), flush=True)
             return
         if args.workload == "batch2d":
             if R.rank == 0:

@@ -37,7 +37,8 @@ enum {
     MLAU_ERR_CUDA = -2,        /* CUDA runtime error */
     MLAU_ERR_NOMEM = -3,       /* device memory exhausted / over budget */
     MLAU_ERR_STATE = -4,       /* NaN or non-positive density/pressure seen */
-    MLAU_ERR_TIMEOUT = -5      /* a bounded device-side wait gave up */
+    MLAU_ERR_TIMEOUT = -5,     /* a bounded device-side wait gave up */
+    MLAU_ERR_CONVERGE = -6     /* an iterative solve ran out of sweeps */
 };
 
 /* Riemann solvers of include/mhd_flux.h. */
@@ -85,6 +86,31 @@ void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en
 void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,
                  double *bz, double bx, double dt, double dx, int nx, int xoff, double gamma);
 
+/* Replace the MRX problem's resistive diffusion of the CT field (uniform
+ * resistivity eta0; energy updated by the resistive Poynting flux) and its
+ * viscous term (uniform kinematic viscosity nu0), 2D/MPI/MRX/myfunc.h:12-22,
+ * 2D/MPI/MRX/mhd_fd_ct_2d.c:726-1174, caller 2D/MPI/MRX/main.cpp:52-68.
+ * Each is an explicit SSP-RK update with the 2D drop-in's scheme (odr, nrk)
+ * and the problem's tables (each axis all zero or all nonzero); the MRX
+ * hyperbolic step itself is mhd_fd_ct_2d_mpi with reconstruction code 5.
+ * mpi_numx = mpi_numy = 1 required. */
+void diff_ctfield_e(double *en, double *bx, double *by, double *bz, double eta0, double dt,
+                    double dx, double dy, int nx, int ny, int xoff, int yoff, double gamma,
+                    int mpi_rank, int mpi_numx, int mpi_numy);
+void ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, double *en, double nu0,
+                   double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                   double gamma, int mpi_rank, int mpi_numx, int mpi_numy);
+/* Replaces the MRX problem's anisotropic heat conduction along B (conductivity
+ * kk0; 2D/MPI/MRX/myfunc.h:34-39, mhd_fd_ct_2d.c:1176-1456): Crank-Nicolson
+ * in p/rho solved by six-colour Gauss-Seidel sweeps (at most 2048, the
+ * reference's CMAX).  Like the reference, it halts the process (messages on
+ * stdout, exit status 255) when the sweeps do not converge; the handle API
+ * returns MLAU_ERR_CONVERGE instead. */
+void t_conduction(const double *ro, const double *mx, const double *my, const double *mz,
+                  double *en, const double *bx, const double *by, const double *bz, double kk0,
+                  double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                  double gamma, int mpi_rank, int mpi_numx, int mpi_numy);
+
 /* The reference fixes the spatial order (ODR), Runge-Kutta order (R_K) and
  * Riemann solver (func_flux=) at compile time in each driver copy
  * (mhd_fd_ct_3d.c:25-27,131-138).  The drop-in drivers read them from here
@@ -126,7 +152,7 @@ int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, i
                     int nrk, int precision);
 int mlau_sim_destroy(mlau_sim *sim);
 /* Host arrays in the order (ro, mx, my, mz, en, bx, by, bz); in 1D bx is
- * unused (set it with mlau_sim_set_bx_1d). */
+ * unused (set it with mlau_sim_set_bx_1d).  A null entry is skipped. */
 int mlau_sim_upload(mlau_sim *sim, const double *const *host8);
 int mlau_sim_download(mlau_sim *sim, double *const *host8);
 int mlau_sim_set_bx_1d(mlau_sim *sim, double bx);
@@ -138,6 +164,18 @@ int mlau_sim_set_bc_1d(mlau_sim *sim, int bc);
  * shock-sensor and cell-B fills inside the step.  All zero (the default) is
  * periodic.  The drop-in 2D drivers apply the problem's own tables. */
 int mlau_sim_set_bc_2d(mlau_sim *sim, const int *dnx, const int *dny);
+/* The MRX operators on a device-resident 2D FP64 state (the simulation's
+ * odr and nrk, its tables; each axis's entries all zero or all nonzero):
+ * resistive diffusion of B with energy, and viscosity of the velocity with
+ * energy.  Enqueued on the simulation's stream like a step. */
+int mlau_sim_resistive_2d(mlau_sim *sim, double eta0, double dt);
+int mlau_sim_viscous_2d(mlau_sim *sim, double nu0, double dt);
+/* Anisotropic heat conduction along B over dt (energy updated; 2D FP64, same
+ * table rule).  *sweeps (may be NULL) receives the Gauss-Seidel sweep count;
+ * MLAU_ERR_CONVERGE after 2048 sweeps without convergence, with the energy
+ * as the reference leaves it.  Synchronises the simulation's stream once per
+ * 8 sweeps to test convergence. */
+int mlau_sim_conduction_2d(mlau_sim *sim, double kk0, double dt, int *sweeps);
 /* nsteps full RK steps with fixed dt, enqueued on the simulation's stream. */
 int mlau_sim_step(mlau_sim *sim, double dt, int nsteps);
 /* CFL time step (3D/MPI/OTvortex/cflcheck.hpp:1-39, 2D cflcheck.hpp,

@@ -50,6 +50,9 @@ def _bind(lib):
     lib.mlau_sim_set_bc_1d.argtypes = [vp, i]
     lib.mlau_sim_set_bc_2d.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
     lib.mlau_sim_step.argtypes = [vp, d, i]
+    lib.mlau_sim_resistive_2d.argtypes = [vp, d, d]
+    lib.mlau_sim_viscous_2d.argtypes = [vp, d, d]
+    lib.mlau_sim_conduction_2d.argtypes = [vp, d, d, C.POINTER(i)]
     lib.mlau_sim_cfl.argtypes = [vp, d, d, d, d, pd, pd]
     lib.mlau_sim_sync.argtypes = [vp]
     lib.mlau_sim_stream.argtypes = [vp]
@@ -100,6 +103,12 @@ def _bind(lib):
     lib.mhd_fd_ct_2d.argtypes = [pd] * 8 + [d] * 3 + [i] * 4 + [d]
     lib.mhd_fd_ct_2d.restype = None
     lib.mhd_fd4c_1d.argtypes = [pd] * 7 + [d] * 3 + [i, i, d]
+    lib.diff_ctfield_e.argtypes = [pd] * 4 + [d] * 4 + [i] * 4 + [d] + [i] * 3
+    lib.diff_ctfield_e.restype = None
+    lib.ns_viscous_2d.argtypes = [pd] * 5 + [d] * 4 + [i] * 4 + [d] + [i] * 3
+    lib.ns_viscous_2d.restype = None
+    lib.t_conduction.argtypes = [pd] * 8 + [d] * 4 + [i] * 4 + [d] + [i] * 3
+    lib.t_conduction.restype = None
     lib.mhd_fd4c_1d.restype = None
     return lib
 
@@ -317,6 +326,22 @@ class Sim:
 
     def step(self, dt: float, nsteps: int = 1):
         _check(lib().mlau_sim_step(self._h, dt, nsteps))
+
+    def resistive(self, eta0: float, dt: float):
+        """Resistive diffusion of B (with the energy) over dt, 2D FP64."""
+        _check(lib().mlau_sim_resistive_2d(self._h, eta0, dt))
+
+    def viscous(self, nu0: float, dt: float):
+        """Viscosity of the velocity (with the energy) over dt, 2D FP64."""
+        _check(lib().mlau_sim_viscous_2d(self._h, nu0, dt))
+
+    def conduction(self, kk0: float, dt: float) -> int:
+        """Anisotropic heat conduction along B over dt, 2D FP64; returns the
+        Gauss-Seidel sweep count (MlauError when 2048 sweeps did not
+        converge; the energy is then as the reference leaves it)."""
+        n = C.c_int(0)
+        _check(lib().mlau_sim_conduction_2d(self._h, kk0, dt, C.byref(n)))
+        return n.value
 
     def sync(self):
         _check(lib().mlau_sim_sync(self._h))

@@ -39,6 +39,7 @@ UNITS = {
     "batch2d_plain.cu": EXACT,
     "batch1d_plain.cu": EXACT,
     "dataio.cu": EXACT,
+    "diff2d.cu": EXACT,
     "cxx_linkage.cpp": [],
 }
 

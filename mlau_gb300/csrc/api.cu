@@ -2,6 +2,7 @@
 // drivers (declared in include/mlau_gb300.h).
 #include <cmath>
 #include <cstdarg>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -179,6 +180,7 @@ int mlau_sim_destroy(mlau_sim *s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     s->timer.recs.clear();
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    diff2d_free(s);
     if (s->sp) split3d_free(s);
     for (void *p : s->allocs) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -192,7 +194,7 @@ int mlau_sim_upload(mlau_sim *s, const double *const *h)
 {
     if (!s || !h) { set_error("null argument"); return MLAU_ERR_ARG; }
     for (int v = 0; v < nvars(s); v++) {
-        if (s->g.dim == 1 && v == 5) continue;
+        if ((s->g.dim == 1 && v == 5) || !h[v]) continue;
         MLAU_CUDA(cudaMemcpyAsync(s->f.s[v], h[v], sizeof(double) * s->g.n,
                                   cudaMemcpyHostToDevice, s->stream));
     }
@@ -203,7 +205,7 @@ int mlau_sim_download(mlau_sim *s, double *const *h)
 {
     if (!s || !h) { set_error("null argument"); return MLAU_ERR_ARG; }
     for (int v = 0; v < nvars(s); v++) {
-        if (s->g.dim == 1 && v == 5) continue;
+        if ((s->g.dim == 1 && v == 5) || !h[v]) continue;
         MLAU_CUDA(cudaMemcpyAsync(h[v], s->f.s[v], sizeof(double) * s->g.n,
                                   cudaMemcpyDeviceToHost, s->stream));
     }
@@ -326,6 +328,24 @@ int mlau_sim_step(mlau_sim *s, double dt, int nsteps)
         if (rc != MLAU_OK) return rc;
     }
     return MLAU_OK;
+}
+
+int mlau_sim_resistive_2d(mlau_sim *s, double eta0, double dt)
+{
+    if (!s || !(dt == dt) || !(eta0 == eta0)) { set_error("bad arguments"); return MLAU_ERR_ARG; }
+    return diff2d_resistive(s, eta0, dt);
+}
+
+int mlau_sim_viscous_2d(mlau_sim *s, double nu0, double dt)
+{
+    if (!s || !(dt == dt) || !(nu0 == nu0)) { set_error("bad arguments"); return MLAU_ERR_ARG; }
+    return diff2d_viscous(s, nu0, dt);
+}
+
+int mlau_sim_conduction_2d(mlau_sim *s, double kk0, double dt, int *sweeps)
+{
+    if (!s || !(dt == dt) || !(kk0 == kk0)) { set_error("bad arguments"); return MLAU_ERR_ARG; }
+    return diff2d_conduction(s, kk0, dt, sweeps);
 }
 
 int mlau_sim_cfl(mlau_sim *s, double cfl, double dr, double vfast, double dt_old, double *dt_out,
@@ -644,6 +664,84 @@ void mhd_fd_ct_2d_mpi(double *ro, double *mx, double *my, double *mz, double *en
         return;
     }
     dropin_2d(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma, true);
+}
+
+// MRX operators (2D/MPI/MRX/mhd_fd_ct_2d.c:726-1174, caller
+// 2D/MPI/MRX/main.cpp:52-68): the same cached 2D context as the step, its
+// scheme (odr, nrk) and the problem's tables; only the arrays an operator
+// reads are uploaded and only those it changes come back.
+enum { MRX_RESISTIVE, MRX_VISCOUS, MRX_CONDUCTION };
+
+static int dropin_mrx(const char *who, double *const *h, const bool *back, double dt, double dx,
+                      double dy, int nx, int ny, int xoff, int yoff, double gamma, int mpi_rank,
+                      int mpi_numx, int mpi_numy, double coef, int op)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mpi_rank != 0 || mpi_numx != 1 || mpi_numy != 1) {
+        set_error("single-GPU build: mpi_rank=0 and mpi_num{x,y}=1 required");
+        report(who);
+        return MLAU_ERR_ARG;
+    }
+    static const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int *tx = dnxs ? dnxs : zero, *ty = dnys ? dnys : zero;
+    mlau_sim *c = get_ctx(2, nx, ny, 1, xoff, yoff, 0, dx, dy, 1.0, gamma);
+    int rc = c ? mlau_sim_set_bc_2d(c, tx, ty) : MLAU_ERR_NOMEM;
+    if (rc == MLAU_OK) rc = mlau_sim_upload(c, (const double *const *)h);
+    if (rc == MLAU_OK) {
+        if (op == MRX_RESISTIVE) rc = diff2d_resistive(c, coef, dt);
+        else if (op == MRX_VISCOUS) rc = diff2d_viscous(c, coef, dt);
+        else rc = diff2d_conduction(c, coef, dt, nullptr);
+    }
+    if (rc == MLAU_OK || rc == MLAU_ERR_CONVERGE) {
+        double *out[8];
+        for (int v = 0; v < 8; v++) out[v] = back[v] ? h[v] : nullptr;
+        const int rd = mlau_sim_download(c, out);
+        if (rd != MLAU_OK) rc = rd;
+    }
+    if (rc != MLAU_OK && rc != MLAU_ERR_CONVERGE) report(who);
+    return rc;
+}
+
+void diff_ctfield_e(double *en, double *bx, double *by, double *bz, double eta0, double dt,
+                    double dx, double dy, int nx, int ny, int xoff, int yoff, double gamma,
+                    int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    double *h[8] = {nullptr, nullptr, nullptr, nullptr, en, bx, by, bz};
+    static const bool back[8] = {false, false, false, false, true, true, true, true};
+    dropin_mrx("diff_ctfield_e", h, back, dt, dx, dy, nx, ny, xoff, yoff, gamma, mpi_rank,
+               mpi_numx, mpi_numy, eta0, MRX_RESISTIVE);
+}
+
+void ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, double *en, double nu0,
+                   double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                   double gamma, int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    double *h[8] = {const_cast<double *>(ro), mx, my, mz, en, nullptr, nullptr, nullptr};
+    static const bool back[8] = {false, true, true, true, true, false, false, false};
+    dropin_mrx("ns_viscous_2d", h, back, dt, dx, dy, nx, ny, xoff, yoff, gamma, mpi_rank,
+               mpi_numx, mpi_numy, nu0, MRX_VISCOUS);
+}
+
+// Non-convergence within CMAX sweeps halts the run, as the reference does
+// (:1447-1453: the two messages, then MPI_Abort with -1), after the energy
+// has been written back.
+void t_conduction(const double *ro, const double *mx, const double *my, const double *mz,
+                  double *en, const double *bx, const double *by, const double *bz, double kk0,
+                  double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                  double gamma, int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    double *h[8] = {const_cast<double *>(ro), const_cast<double *>(mx),
+                    const_cast<double *>(my), const_cast<double *>(mz), en,
+                    const_cast<double *>(bx), const_cast<double *>(by), const_cast<double *>(bz)};
+    static const bool back[8] = {false, false, false, false, true, false, false, false};
+    const int rc = dropin_mrx("t_conduction", h, back, dt, dx, dy, nx, ny, xoff, yoff, gamma,
+                              mpi_rank, mpi_numx, mpi_numy, kk0, MRX_CONDUCTION);
+    if (rc == MLAU_ERR_CONVERGE) {
+        puts("Heat conduction did not converge. Calculation halted.");
+        puts("Try relaxing threshold.");
+        fflush(stdout);
+        exit(255);
+    }
 }
 
 void mhd_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, double *by,

@@ -18,6 +18,16 @@ extern "C" void mlau_c_fd_ct_2d(double *, double *, double *, double *, double *
 extern "C" void mlau_c_fd_ct_2d_mpi(double *, double *, double *, double *, double *, double *,
                                     double *, double *, double, double, double, int, int, int,
                                     int, double, int, int, int) __asm__("mhd_fd_ct_2d_mpi");
+extern "C" void mlau_c_diff_ctfield_e(double *, double *, double *, double *, double, double,
+                                      double, double, int, int, int, int, double, int, int, int)
+    __asm__("diff_ctfield_e");
+extern "C" void mlau_c_ns_viscous_2d(const double *, double *, double *, double *, double *,
+                                     double, double, double, double, int, int, int, int, double,
+                                     int, int, int) __asm__("ns_viscous_2d");
+extern "C" void mlau_c_t_conduction(const double *, const double *, const double *,
+                                    const double *, double *, const double *, const double *,
+                                    const double *, double, double, double, double, int, int,
+                                    int, int, double, int, int, int) __asm__("t_conduction");
 extern "C" void mlau_c_fd4c_1d(double *, double *, double *, double *, double *, double *,
                                double *, double, double, double, int, int, double)
     __asm__("mhd_fd4c_1d");
@@ -46,6 +56,34 @@ void mhd_fd_ct_2d(double *ro, double *mx, double *my, double *mz, double *en, do
                   int xoff, int yoff, double gamma, int mpi_rank, int mpi_numx, int mpi_numy)
 {
     mlau_c_fd_ct_2d_mpi(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, nx, ny, xoff, yoff, gamma,
+                        mpi_rank, mpi_numx, mpi_numy);
+}
+
+// 2D/MPI/MRX/myfunc.h:12-16
+void diff_ctfield_e(double *en, double *bx, double *by, double *bz, double eta0, double dt,
+                    double dx, double dy, int nx, int ny, int xoff, int yoff, double gamma,
+                    int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    mlau_c_diff_ctfield_e(en, bx, by, bz, eta0, dt, dx, dy, nx, ny, xoff, yoff, gamma, mpi_rank,
+                          mpi_numx, mpi_numy);
+}
+
+// 2D/MPI/MRX/myfunc.h:17-22
+void ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, double *en, double nu0,
+                   double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                   double gamma, int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    mlau_c_ns_viscous_2d(ro, mx, my, mz, en, nu0, dt, dx, dy, nx, ny, xoff, yoff, gamma, mpi_rank,
+                         mpi_numx, mpi_numy);
+}
+
+// 2D/MPI/MRX/myfunc.h:34-39
+void t_conduction(const double *ro, const double *mx, const double *my, const double *mz,
+                  double *en, const double *bx, const double *by, const double *bz, double kk0,
+                  double dt, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                  double gamma, int mpi_rank, int mpi_numx, int mpi_numy)
+{
+    mlau_c_t_conduction(ro, mx, my, mz, en, bx, by, bz, kk0, dt, dx, dy, nx, ny, xoff, yoff, gamma,
                         mpi_rank, mpi_numx, mpi_numy);
 }
 

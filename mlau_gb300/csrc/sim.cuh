@@ -48,6 +48,13 @@ struct Sim {
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0.0;
     int graph_steps = 0;
+    // anisotropic conduction: device convergence state with its pinned host
+    // copy, and the captured graph of a run of Gauss-Seidel sweeps with the
+    // parameters it was captured for
+    void *d_cond = nullptr;
+    void *h_cond = nullptr;
+    cudaGraphExec_t cond_exec = nullptr;
+    long long cond_key = -1;
 };
 
 int plain3d_alloc(Sim *s);
@@ -60,6 +67,10 @@ int split3d_alloc(Sim *s);
 int split3d_step(Sim *s, double dt);
 void split3d_free(Sim *s);
 int split3d_check(Sim *s);
+int diff2d_resistive(Sim *s, double eta0, double dt);
+int diff2d_viscous(Sim *s, double nu0, double dt);
+int diff2d_conduction(Sim *s, double kk0, double dt, int *sweeps);
+void diff2d_free(Sim *s);
 int cfl_compute(Sim *s, double *vmax_out);
 int launches_per_step(const Sim *s);
 

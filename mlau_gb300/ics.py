@@ -13,6 +13,8 @@ x fastest, ``off`` ghost cells per side, ghosts filled periodically) for:
 * ``turbulence_3d`` - a periodic [0,1]^3 box: rho=1 with a 1% random-phase
   perturbation (|k|<=6), solenoidal random-phase velocity at a given rms sonic
   Mach, B = B0 + curl A with A at 10% of |B0|, beta=1 w.r.t. |B0|^2.
+* ``mrx_2d`` - the reference's magnetic-reconnection problem (Harris sheet,
+  2048 x 256 cells, x periodic, y walls), seeded where it seeds from the clock.
 
 Face-centred B is built as the discrete curl of an edge-centred vector
 potential with the scheme's own face-to-centre difference (2-point for
@@ -192,6 +194,49 @@ def turbulence_2d(n=512, seed=0, off=4, gamma=5.0 / 3.0, odr=4, ny=None, vrms=0.
     return st, meta
 
 
+MRX_TABLES = ((0,) * 8, (1, 1, -1, 1, 1, 1, -1, 1))  # 2D/MPI/MRX/global.hpp:22-23
+
+
+def mrx_2d(n=2048, ny=256, seed=0, off=4, gamma=5.0 / 3.0, lx=128.0, lam=1.0, beta=0.2, b0=1.0,
+           b1=0.05, dv=0.01, ro0=1.0, ro1=1.0, cfl=0.2):
+    """Magnetic reconnection (2D/MPI/MRX/init.hpp:11-76, global.hpp:11-75):
+    a Harris current sheet Bx = b0 tanh(y/lam), density (ro0-ro1) sech^2 + ro1
+    in pressure balance with lobe beta, the X-point perturbation of amplitude
+    b1 on the face fields, and a random Vy of amplitude dv per column damped
+    as exp(-y^2/4lam^2).  The reference seeds that noise from the clock; here
+    it comes from `seed`.  Every cell, ghosts included, takes the analytic
+    value, as the reference's initialiser does.  Periodic in x, walls in y
+    (MRX_TABLES); the diffusion coefficients eta0 = nu0 = lam/500."""
+    nx_, ny_ = n + 2 * off, ny + 2 * off
+    ly = lx * ny / n
+    dx, dy = lx / n, ly / ny
+    x = (np.arange(nx_) - off + 0.5) * dx - 0.5 * lx
+    y = (np.arange(ny_) - off + 0.5) * dy - 0.5 * ly
+    xm, ym = x - 0.5 * dx, y - 0.5 * dy
+    X, Y = np.meshgrid(x, y)
+    XM, YM = np.meshgrid(xm, ym)
+    rng = np.random.default_rng(seed)
+    dvy = rng.uniform(-dv, dv, nx_)
+    ro = (ro0 - ro1) / np.cosh(Y / (lam + 1e-15)) ** 2 + ro1
+    vy = dvy[None, :] * np.exp(-(Y * Y) / (4 * lam * lam))
+    bxh = b0 * np.tanh(Y / (lam + 1e-15))
+    pr = 0.5 * ((1.0 + beta) * b0 * b0 - bxh * bxh)
+    bx = bxh - b1 * (Y / lam) * np.exp(-(XM * XM + Y * Y) / (4 * lam * lam))
+    by = b1 * (X / lam) * np.exp(-(X * X + YM * YM) / (4 * lam * lam))
+    g = np.exp(-(X * X + Y * Y) / (4 * lam * lam))
+    bxc = bxh - b1 * (Y / lam) * g
+    byc = b1 * (X / lam) * g
+    en = pr / (gamma - 1) + 0.5 * (ro * vy * vy + bxc * bxc + byc * byc)
+    z = np.zeros_like(ro)
+    st = {"ro": ro, "mx": z.copy(), "my": ro * vy, "mz": z.copy(), "en": en, "bx": bx, "by": by,
+          "bz": z.copy()}
+    st = {k: np.ascontiguousarray(a, dtype=np.float64) for k, a in st.items()}
+    vfast = float(np.sqrt((0.5 * gamma * beta * b0 * b0 + b0 * b0) / ro0))
+    dr = min(dx, dy)
+    return st, dict(dx=dx, dy=dy, gamma=gamma, off=off, vfast=vfast, cfl=cfl, dr=dr,
+                    dt=cfl * dr / vfast, eta0=lam / 5e2, nu0=lam / 5e2, tables=MRX_TABLES)
+
+
 def riemann_1d(n=2048, seed=0, off=4, gamma=2.0):
     """Config-1 workload: seeded 1D Riemann problem on [0,1]; returns (state, meta)."""
     rng = np.random.default_rng(seed)
@@ -238,7 +283,11 @@ def div_b_3d(st, dx, dy, dz, off=4, odr=4):
     return float(np.abs(div[sl]).max() * min(dx, dy, dz) / bmax)
 
 
-def div_b_2d(st, dx, dy, off=4, odr=4):
+def div_b_2d(st, dx, dy, off=4, odr=4, base=None):
+    """max |div B| * dx / max|B| over interior cells with the scheme
+    difference; with `base`, the change of div B from that state instead
+    (a CT update keeps it at round-off when the initial field is not
+    discretely solenoidal)."""
     def d(f, ax, h):
         f1 = f
         f2 = np.roll(f, -1, axis=ax)
@@ -247,6 +296,8 @@ def div_b_2d(st, dx, dy, off=4, odr=4):
         f0, f3 = np.roll(f, 1, axis=ax), np.roll(f, -2, axis=ax)
         return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0 / h
     div = d(st["bx"], 1, dx) + d(st["by"], 0, dy)
+    if base is not None:
+        div = div - (d(base["bx"], 1, dx) + d(base["by"], 0, dy))
     sl = (slice(off, -off),) * 2
     bmax = max(np.abs(st[k][sl]).max() for k in ("bx", "by"))
     return float(np.abs(div[sl]).max() * min(dx, dy) / bmax)

@@ -51,6 +51,10 @@ class Port:
             lib.oracle_diff_ctfield_e.restype = None
             lib.oracle_ns_viscous_2d.argtypes = [_cdp] + [_dp] * 4 + [d, d, d, d, i, i, i, i, d, i, i, pi8, pi8]
             lib.oracle_ns_viscous_2d.restype = None
+            lib.oracle_t_conduction.argtypes = ([_cdp] * 4 + [_dp] + [_cdp] * 3
+                                                + [d, d, d, d, i, i, i, i, d, i, pi8, pi8, i,
+                                                   C.POINTER(i)])
+            lib.oracle_t_conduction.restype = i
             lib.oracle_fd4c_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d, i, i, i, i]
             lib.oracle_fd4c_1d.restype = None
             lib.oracle_cfl_3d.argtypes = [_cdp] * 8 + [i] * 6 + [d, d, d, d, d, C.POINTER(d)]
@@ -98,6 +102,20 @@ class Port:
         tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
         cls.lib().oracle_ns_viscous_2d(s["ro"], s["mx"], s["my"], s["mz"], s["en"], nu0, dt, dx,
                                        dy, nx, ny, off, off, gamma, odr, nrk, tab(dnx), tab(dny))
+
+    @classmethod
+    def conduction2d(cls, s, kk0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, dnx=None, dny=None,
+                     cmax=2048):
+        """t_conduction of the MRX driver file, in place on en; returns
+        (Gauss-Seidel sweeps, err) with err -1 when cmax sweeps ran."""
+        ny, nx = s["ro"].shape
+        tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
+        err = C.c_int(0)
+        n = cls.lib().oracle_t_conduction(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by",
+                                                           "bz")],
+                                          kk0, dt, dx, dy, nx, ny, off, off, gamma, odr, tab(dnx),
+                                          tab(dny), cmax, C.byref(err))
+        return n, err.value
 
     @classmethod
     def setbc2d(cls, s, dnx, dny, off=4):
@@ -220,7 +238,9 @@ class RefMRX:
             lib.ref_mrx_step.argtypes = [_dp] * 8 + [d, d, d, i, i, i, i, d]
             lib.ref_diff_ctfield_e.argtypes = [_dp] * 4 + [d, d, d, d, i, i, i, i, d]
             lib.ref_ns_viscous_2d.argtypes = [_dp] * 5 + [d, d, d, d, i, i, i, i, d]
-            for f in (lib.ref_mrx_step, lib.ref_diff_ctfield_e, lib.ref_ns_viscous_2d):
+            lib.ref_t_conduction.argtypes = [_dp] * 8 + [d, d, d, d, i, i, i, i, d]
+            for f in (lib.ref_mrx_step, lib.ref_diff_ctfield_e, lib.ref_ns_viscous_2d,
+                      lib.ref_t_conduction):
                 f.restype = None
             cls._libs[key] = lib
         return cls._libs[key]
@@ -261,3 +281,14 @@ class RefMRX:
         lib = cls._get(odr, nrk)
         cls._call(lib.ref_ns_viscous_2d, lib, dnx, dny, s["ro"], s["mx"], s["my"], s["mz"], s["en"],
                   nu0, dt, dx, dy, nx, ny, off, off, gamma)
+
+    @classmethod
+    def conduction2d(cls, s, kk0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None,
+                     dny=None):
+        """The reference's t_conduction (it aborts the process when the sweeps
+        do not converge within its CMAX of 2048: keep cases convergent)."""
+        ny, nx = s["ro"].shape
+        lib = cls._get(odr, nrk)
+        cls._call(lib.ref_t_conduction, lib, dnx, dny,
+                  *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                  kk0, dt, dx, dy, nx, ny, off, off, gamma)

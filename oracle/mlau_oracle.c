@@ -1145,3 +1145,191 @@ void oracle_ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, 
     free(ir); free(ut); free(fx); free(fy);
 }
 #undef S2
+
+/* ---- anisotropic thermal conduction (2D/MPI/MRX/mhd_fd_ct_2d.c:1176-1456) ---- */
+
+/* Periodic ghost exchange of one rank (mpi_sdrv2d, 2D/MPI/MRX/boundary.c:31-141):
+   along an axis whose table entry 0 is zero. */
+static void o_sdrv2d(double **p, int nn, int dnx0, int dny0, int nx, int ny, int xoff, int yoff)
+{
+    static const int z[8] = {0, 0, 0, 0, 0, 0, 0, 0};  /* no mirrors: periodic fills only */
+    o_bc2d_mpi(p, nn, z, z, z, z, dnx0, dny0, nx, ny, xoff, yoff);
+}
+
+/* Mirror of one array along x / y (mpi_xbc2d / mpi_ybc2d, boundary.c:143-185):
+   nothing when dn is zero. */
+static void o_xbc2d(double *f, int nx, int ny, int xoff, int st, int dn)
+{
+    if (dn == 0) return;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < xoff; i++) f[(long)nx * j + i] = dn * f[(long)nx * j + (2 * xoff - 1 + st) - i];
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < xoff - st; i++)
+            f[(long)nx * j + (nx - 1 - i)] = dn * f[(long)nx * j + (nx - 2 * xoff + st) + i];
+}
+
+static void o_ybc2d(double *f, int nx, int ny, int yoff, int st, int dn)
+{
+    if (dn == 0) return;
+    for (int j = 0; j < yoff; j++)
+        for (int i = 0; i < nx; i++) f[(long)nx * j + i] = dn * f[(long)nx * ((2 * yoff - 1 + st) - j) + i];
+    for (int j = 0; j < yoff - st; j++)
+        for (int i = 0; i < nx; i++)
+            f[(long)nx * (ny - 1 - j) + i] = dn * f[(long)nx * ((ny - 2 * yoff + st) + j) + i];
+}
+
+/* mhd_e2p (:1176-1219): total energy -> pressure (direc +1) or back (-1) over
+   [1, nx-2) x [1, ny-2), then the energy's boundary fill. */
+static void o_e2p(const double *ro, const double *mx, const double *my, const double *mz,
+                  double *en, const double *bx, const double *by, const double *bz, int nx,
+                  int ny, int xoff, int yoff, double gamma, int direc, int odr, const int *dnx,
+                  const int *dny)
+{
+    for (int j = 1; j < ny - 2; j++)
+        for (int i = 1; i < nx - 2; i++) {
+            const long s = (long)nx * j + i;
+            const double iro = 1.0 / ro[s];
+            const double vx = mx[s] * iro, vy = my[s] * iro, vz = mz[s] * iro;
+            const double bxc = o_face2cen(odr, bx[s - 1], bx[s], bx[s + 1], bx[s + 2]);
+            const double byc = o_face2cen(odr, by[s - nx], by[s], by[s + nx], by[s + 2 * nx]);
+            const double bzc = bz[s];
+            const double v2 = (vx * vx + vy * vy + vz * vz);
+            const double b2 = (bxc * bxc + byc * byc + bzc * bzc);
+            const double t0 = (gamma - 1) * (en[s] - 0.5 * (ro[s] * v2 + b2));
+            const double t1 = en[s] / (gamma - 1) + 0.5 * (ro[s] * v2 + b2);
+            en[s] = 0.5 * ((1 + direc) * t0 + (1 - direc) * t1);
+        }
+    o_sdrv2d(&en, 1, dnx[0], dny[0], nx, ny, xoff, yoff);
+    o_xbc2d(en, nx, ny, xoff, 0, dnx[4]);
+    o_ybc2d(en, nx, ny, yoff, 0, dny[4]);
+}
+
+/* diffusion2d_ani (:1221-1378): Crank-Nicolson step of
+   g df/dt = div(g K grad f) with the full tensor K, solved by six-colour
+   Gauss-Seidel sweeps until the summed |residual| falls below 1e-6 of the
+   summed |rhs/denominator| or cmax sweeps ran.  The colours are independent
+   sets of the stencil, so the sweep equals the reference's loop order.
+   Returns the number of sweeps; *err = -1 when it reached cmax. */
+static int o_diffusion2d_ani(double *f, const double *g, double *kxx, double *kyy, double *kxy,
+                             double dt0, double dx, double dy, int nx, int ny, int xoff, int yoff,
+                             int stx, int dnx, int sty, int dny, int dnx0, int dny0, int odr,
+                             int cmax, int *err)
+{
+    const int od4 = (o_lin_odr(odr) - 1) / 2;
+    const double idx2 = 1.0 / (dx * dx), idy2 = 1.0 / (dy * dy), idxy = 1.0 / (dx * dy);
+    const double alpha = 0.5, beta = 1.0 - alpha, omega = 1.0, eps = 1e-6;
+    const double d1 = 1.0 + 0.25 * od4, d2 = 1.0 * od4 / 12.0;
+    const long n = (long)nx * ny;
+    double *denom = alloc_d(n), *ig = alloc_d(n), *rhs = alloc_d(n);
+    double anorm, anorm_f = 0.0;
+    int cnt = 0;
+    for (long s = 0; s < n; s++) {
+        ig[s] = 1.0 / g[s];
+        kxx[s] *= g[s];
+        kyy[s] *= g[s];
+        kxy[s] *= g[s];
+    }
+#define F(a, b) f[(long)nx * (b) + (a)]
+    for (int j = 2; j < ny - 2; j++)
+        for (int i = 2; i < nx - 2; i++) {
+            const long s = (long)nx * j + i, sim = s - 1, sip = s + 1, sjm = s - nx, sjp = s + nx;
+            const double k0 = 0.5 * (kxx[sim] + kxx[s]), k1 = 0.5 * (kxx[sip] + kxx[s]);
+            const double k2 = 0.5 * (kyy[sjm] + kyy[s]), k3 = 0.5 * (kyy[sjp] + kyy[s]);
+            const double dt = dt0 * ig[s];
+            denom[s] = 1.0 / (1.0 + alpha * dt * d1 * (idx2 * (k0 + k1) + idy2 * (k2 + k3)));
+            rhs[s] = f[s] + beta * dt *
+                     ((+idx2 * (+k0 * (d1 * (f[sim] - f[s]) - d2 * (f[s - 2] - f[sip]))
+                                + k1 * (d1 * (f[sip] - f[s]) - d2 * (f[s + 2] - f[sim])))
+                       + idy2 * (+k2 * (d1 * (f[sjm] - f[s]) - d2 * (f[s - 2 * nx] - f[sjp]))
+                                 + k3 * (d1 * (f[sjp] - f[s]) - d2 * (f[s + 2 * nx] - f[sjm]))))
+                      + 0.25 * (+idxy * (+kxy[sjm] * (F(i - 1, j - 1) - F(i + 1, j - 1))
+                                         + kxy[sjp] * (F(i + 1, j + 1) - F(i - 1, j + 1))
+                                         + kxy[sim] * (F(i - 1, j - 1) - F(i - 1, j + 1))
+                                         + kxy[sip] * (F(i + 1, j + 1) - F(i + 1, j - 1)))));
+            anorm_f += fabs(rhs[s] * denom[s]);
+        }
+    do {
+        anorm = 0.0;
+        for (int py = 0; py < 2; py++)
+            for (int px = 0; px < 3; px++)
+                for (int j = 2 + py; j < ny - 2; j += 2)
+                    for (int i = 4 - ((j + px) % 3); i < nx - 2; i += 3) {
+                        const long s = (long)nx * j + i, sim = s - 1, sip = s + 1, sjm = s - nx,
+                                   sjp = s + nx;
+                        const double k0 = 0.5 * (kxx[sim] + kxx[s]), k1 = 0.5 * (kxx[sip] + kxx[s]);
+                        const double k2 = 0.5 * (kyy[sjm] + kyy[s]), k3 = 0.5 * (kyy[sjp] + kyy[s]);
+                        const double dt = dt0 * ig[s];
+                        const double resid =
+                            (alpha * dt *
+                                 ((+idx2 * (+k0 * (d1 * f[sim] - d2 * (f[s - 2] - f[sip]))
+                                            + k1 * (d1 * f[sip] - d2 * (f[s + 2] - f[sim])))
+                                   + idy2 * (+k2 * (d1 * f[sjm] - d2 * (f[s - 2 * nx] - f[sjp]))
+                                             + k3 * (d1 * f[sjp] - d2 * (f[s + 2 * nx] - f[sjm]))))
+                                  + 0.25 * (+idxy * (+kxy[sjm] * (F(i - 1, j - 1) - F(i + 1, j - 1))
+                                                     + kxy[sjp] * (F(i + 1, j + 1) - F(i - 1, j + 1))
+                                                     + kxy[sim] * (F(i - 1, j - 1) - F(i - 1, j + 1))
+                                                     + kxy[sip] * (F(i + 1, j + 1) - F(i + 1, j - 1)))))
+                             + rhs[s]) * denom[s] - f[s];
+                        anorm += fabs(resid);
+                        f[s] += omega * resid;
+                    }
+        o_sdrv2d(&f, 1, dnx0, dny0, nx, ny, xoff, yoff);
+        o_xbc2d(f, nx, ny, xoff, stx, dnx);
+        o_ybc2d(f, nx, ny, yoff, sty, dny);
+        cnt++;
+    } while ((anorm > eps * anorm_f) && (cnt < cmax));
+#undef F
+    for (long s = 0; s < n; s++) {
+        kxx[s] *= ig[s];
+        kyy[s] *= ig[s];
+        kxy[s] *= ig[s];
+    }
+    if (cnt == cmax) *err = -1;
+    free(denom); free(ig); free(rhs);
+    return cnt;
+}
+
+/* t_conduction (:1380-1456): anisotropic heat conduction along B with
+   conductivity kk0, implicit (Crank-Nicolson) in the temperature p/rho.
+   Returns the Gauss-Seidel sweep count; *err = -1 when it did not converge
+   within cmax sweeps (the reference then aborts the run). */
+int oracle_t_conduction(const double *ro, const double *mx, const double *my, const double *mz,
+                        double *en, const double *bx, const double *by, const double *bz,
+                        double kk0, double dt, double dx, double dy, int nx, int ny, int xoff,
+                        int yoff, double gamma, int odr, const int *dnx_in, const int *dny_in,
+                        int cmax, int *err)
+{
+    const int *dnx = dnx_in ? dnx_in : o_zero8, *dny = dny_in ? dny_in : o_zero8;
+    const long n = (long)nx * ny;
+    const double eps = 1e-6;
+    double *kxx = alloc_d(n), *kyy = alloc_d(n), *kxy = alloc_d(n);
+    *err = 0;
+    for (int j = 1; j < ny - 2; j++)
+        for (int i = 1; i < nx - 2; i++) {
+            const long s = (long)nx * j + i;
+            const double bxc = o_face2cen(odr, bx[s - 1], bx[s], bx[s + 1], bx[s + 2]);
+            const double byc = o_face2cen(odr, by[s - nx], by[s], by[s + nx], by[s + 2 * nx]);
+            const double bzc = bz[s];
+            const double ib2 = 1.0 / (bxc * bxc + byc * byc + bzc * bzc + eps);
+            kxx[s] = kk0 * (bxc * bxc + eps) * ib2;
+            kyy[s] = kk0 * (byc * byc + eps) * ib2;
+            kxy[s] = kk0 * (bxc * byc) * ib2;
+        }
+    double *p[3] = {kxx, kyy, kxy};
+    o_sdrv2d(p, 3, dnx[0], dny[0], nx, ny, xoff, yoff);
+    o_xbc2d(kxx, nx, ny, xoff, 0, dnx[5] * dnx[5]);
+    o_xbc2d(kyy, nx, ny, xoff, 0, dnx[6] * dnx[6]);
+    o_xbc2d(kxy, nx, ny, xoff, 0, dnx[5] * dnx[6]);
+    o_ybc2d(kxx, nx, ny, yoff, 0, dny[5] * dny[5]);
+    o_ybc2d(kyy, nx, ny, yoff, 0, dny[6] * dny[6]);
+    o_ybc2d(kxy, nx, ny, yoff, 0, dny[5] * dny[6]);
+    o_e2p(ro, mx, my, mz, en, bx, by, bz, nx, ny, xoff, yoff, gamma, +1, odr, dnx, dny);
+    for (long s = 0; s < n; s++) en[s] /= ro[s];
+    const int cnt = o_diffusion2d_ani(en, ro, kxx, kyy, kxy, dt, dx, dy, nx, ny, xoff, yoff, 0, +0,
+                                      0, +1, dnx[0], dny[0], odr, cmax, err);
+    for (long s = 0; s < n; s++) en[s] *= ro[s];
+    o_e2p(ro, mx, my, mz, en, bx, by, bz, nx, ny, xoff, yoff, gamma, -1, odr, dnx, dny);
+    free(kxx); free(kyy); free(kxy);
+    return cnt;
+}
+

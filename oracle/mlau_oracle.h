@@ -108,5 +108,14 @@ void oracle_ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, 
                           double nu0, double dt, double dx, double dy, int nx, int ny, int xoff,
                           int yoff, double gamma, int odr, int nrk, const int *dnx,
                           const int *dny);
+/* Anisotropic heat conduction along B (t_conduction with diffusion2d_ani,
+ * 2D/MPI/MRX/mhd_fd_ct_2d.c:1176-1456): implicit Crank-Nicolson in p/rho by
+ * six-colour Gauss-Seidel; returns the sweep count, *err = -1 when cmax
+ * sweeps did not converge (the reference's CMAX is 2048). */
+int oracle_t_conduction(const double *ro, const double *mx, const double *my, const double *mz,
+                        double *en, const double *bx, const double *by, const double *bz,
+                        double kk0, double dt, double dx, double dy, int nx, int ny, int xoff,
+                        int yoff, double gamma, int odr, const int *dnx, const int *dny,
+                        int cmax, int *err);
 
 #endif

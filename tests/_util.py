@@ -15,7 +15,7 @@ def golden_cases(prefix):
 def load_golden(name):
     """(params dict, input state, {nsteps: output state}) with ghosts rebuilt."""
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
-    dim = int(name[0])
+    dim = int(z["dim"]) if "dim" in z.files else int(name[0])
     prm = {k: (z[k].item() if z[k].ndim == 0 else z[k]) for k in z.files
            if not (k.startswith("in_") or k.startswith("out"))}
 

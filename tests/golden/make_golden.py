@@ -63,6 +63,23 @@ CASES_2D_WALLS = [
     ("2d_hlld_o2_walls", 16, 2, "hlld", 13, (1, -1, 1, 1, 1, -1, 1, 1), (1, 1, -1, 1, 1, 1, -1, 1)),
     ("2d_roe_o4_neumann", 16, 4, "roe", 14, (1,) * 8, (1,) * 8),
 ]
+# The MRX problem's main loop (2D/MPI/MRX/main.cpp:48-68): hyperbolic step,
+# resistive diffusion of B, viscosity and, where kd > 0, anisotropic heat
+# conduction (diffusion number kd; the pressure is perturbed by 10 % so that
+# the temperature varies); its driver file is built with ODR 2 (the
+# MC-limited MUSCL, reconstruction code 5 here) or 4 and R_K 2 or 3; whole
+# arrays stored: (name, nx, ny, ref odr, code, nrk, seed, dnx, dny, kd)
+MRX_TABLES = ((0,) * 8, (1, 1, -1, 1, 1, 1, -1, 1))  # 2D/MPI/MRX/global.hpp:22-23
+WALLS = (1, -1, 1, 1, 1, -1, 1, 1)
+CASES_MRX = [
+    ("mrx2d_o5_rk3", 24, 20, 2, 5, 3, 21, *MRX_TABLES, 0.0),
+    ("mrx2d_o4_rk2", 24, 20, 4, 4, 2, 22, *MRX_TABLES, 0.0),
+    ("mrx2d_o5_rk2_periodic", 20, 20, 2, 5, 2, 23, (0,) * 8, (0,) * 8, 0.0),
+    ("mrx2d_o4_rk3_walls", 20, 24, 4, 4, 3, 24, WALLS, MRX_TABLES[1], 0.0),
+    ("mrx2d_o5_rk3_cond", 24, 20, 2, 5, 3, 25, *MRX_TABLES, 2.0),
+    ("mrx2d_o4_rk3_cond_walls", 20, 24, 4, 4, 3, 26, WALLS, MRX_TABLES[1], 2.0),
+]
+MRX_LOOPS = (1, 3)
 STEPS = (1, 4)
 
 
@@ -145,6 +162,38 @@ def main(only=()):
             done = nstep
             for k, v in s.items():
                 out[f"out{nstep}_" + k] = v.copy()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, nx, ny, rodr, code, nrk, seed, dnx, dny, kd in CASES_MRX:
+        if skip(name):
+            continue
+        from oracle import Port, RefMRX
+        st, m = ics.turbulence_2d(n=nx - 2 * OFF, ny=ny - 2 * OFF, seed=seed, odr=code, vrms=0.4)
+        if kd > 0:
+            rng = np.random.default_rng(seed)
+            st["en"] = st["en"] * (1 + 0.1 * rng.uniform(-1, 1, st["en"].shape))
+        Port.setbc2d(st, dnx, dny)
+        dt = 0.3 * m["dx"] / m["vfast"]
+        # diffusion numbers eta0*dt/dx^2 = 0.05, nu0*dt/dx^2 = 0.04
+        eta0, nu0 = 0.05 * m["dx"] ** 2 / dt, 0.04 * m["dx"] ** 2 / dt
+        kk0 = kd * m["dx"] ** 2 / dt
+        out = {"dim": 2, "dt": dt, "dx": m["dx"], "dy": m["dy"], "gamma": m["gamma"], "odr": code,
+               "nrk": nrk, "eta0": eta0, "nu0": nu0, "kk0": kk0, "dnx": np.array(dnx),
+               "dny": np.array(dny)}
+        for k, v in st.items():
+            out["in_" + k] = v.copy()
+        s = ics.copy_state(st)
+        kw = dict(gamma=m["gamma"], odr=rodr, nrk=nrk, dnx=dnx, dny=dny)
+        done = 0
+        for nloop in MRX_LOOPS:
+            for _ in range(nloop - done):
+                RefMRX.step(s, dt, m["dx"], m["dy"], **kw)
+                RefMRX.resistive2d(s, eta0, dt, m["dx"], m["dy"], **kw)
+                RefMRX.viscous2d(s, nu0, dt, m["dx"], m["dy"], **kw)
+                if kk0 > 0:
+                    RefMRX.conduction2d(s, kk0, dt, m["dx"], m["dy"], **kw)
+            done = nloop
+            for k, v in s.items():
+                out[f"out{nloop}_" + k] = v.copy()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print("wrote golden cases to", HERE)
 

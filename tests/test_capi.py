@@ -46,7 +46,9 @@ def test_cxx_linkage_drivers_exported(gpu_lib):
     for mangled in ("_Z12mhd_fd_ct_3dPdS_S_S_S_S_S_S_ddddiiiiiidiiii",
                     "_Z12mhd_fd_ct_2dPdS_S_S_S_S_S_S_dddiiiid",
                     "_Z12mhd_fd_ct_2dPdS_S_S_S_S_S_S_dddiiiidiii",
-                    "_Z11mhd_fd4c_1dPdS_S_S_S_S_S_dddiid"):
+                    "_Z11mhd_fd4c_1dPdS_S_S_S_S_S_dddiid",
+                    "_Z14diff_ctfield_ePdS_S_S_ddddiiiidiii",
+                    "_Z13ns_viscous_2dPKdPdS1_S1_S1_ddddiiiidiii"):
         assert mangled in syms
 
 

@@ -46,7 +46,89 @@ def test_port_matches_golden_1d(port, name):
         assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
 
 
+def run_mrx_loop(port, s, prm, nloop):
+    """The MRX problem's main loop (2D/MPI/MRX/main.cpp:48-68) on the oracle:
+    hyperbolic step (LHLLD), resistive diffusion, viscosity."""
+    kw = dict(gamma=prm["gamma"], odr=prm["odr"], nrk=prm["nrk"], dnx=prm["dnx"], dny=prm["dny"])
+    for _ in range(nloop):
+        port.step2d(s, prm["dt"], prm["dx"], prm["dy"], flux="lhlld", **kw)
+        port.resistive2d(s, prm["eta0"], prm["dt"], prm["dx"], prm["dy"], **kw)
+        port.viscous2d(s, prm["nu0"], prm["dt"], prm["dx"], prm["dy"], **kw)
+        if prm.get("kk0", 0.0) > 0:
+            n, err = port.conduction2d(s, prm["kk0"], prm["dt"], prm["dx"], prm["dy"],
+                                       **{k: kw[k] for k in ("gamma", "odr", "dnx", "dny")})
+            assert err == 0 and n > 1
+
+
+@pytest.mark.parametrize("name", golden_cases("mrx"))
+def test_port_matches_golden_mrx(port, name):
+    prm, s, outs = load_golden(name)
+    done = 0
+    for n in sorted(outs):
+        run_mrx_loop(port, s, prm, n - done)
+        done = n
+        assert equal_values(s, outs[n]), f"{name}: differs after {n} loops"
+
+
 needs_ref = pytest.mark.skipif(not Ref.available(), reason="reference tree not present")
+
+MRX_TABLES = [((0,) * 8, (0,) * 8), ((0,) * 8, (1, 1, -1, 1, 1, 1, -1, 1)),
+              ((1, -1, 1, 1, 1, -1, 1, 1), (1, 1, -1, 1, 1, 1, -1, 1))]
+
+
+@needs_ref
+@pytest.mark.parametrize("tables", MRX_TABLES)
+@pytest.mark.parametrize("rodr,nrk", [(2, 2), (2, 3), (4, 2), (4, 3)])
+def test_mrx_operators_match_reference(port, rodr, nrk, tables):
+    """Each MRX operator alone against the reference's MRX driver file built
+    with that ODR and R_K (its ODR 2 is reconstruction code 5 here)."""
+    from oracle import RefMRX
+
+    code = 5 if rodr == 2 else 4
+    st, m = ics.turbulence_2d(n=14, ny=10, seed=rodr * 3 + nrk, odr=code, vrms=0.4)
+    port.setbc2d(st, *tables)
+    dt = 0.3 * m["dx"] / m["vfast"]
+    coef = 0.08 * m["dx"] ** 2 / dt
+    kw = dict(gamma=m["gamma"], nrk=nrk, dnx=tables[0], dny=tables[1])
+    for op in ("step", "resistive2d", "viscous2d"):
+        a, b = ics.copy_state(st), ics.copy_state(st)
+        if op == "step":
+            port.step2d(a, dt, m["dx"], m["dy"], odr=code, flux="lhlld", **kw)
+            RefMRX.step(b, dt, m["dx"], m["dy"], odr=rodr, **kw)
+        else:
+            getattr(port, op)(a, coef, dt, m["dx"], m["dy"], odr=code, **kw)
+            getattr(RefMRX, op)(b, coef, dt, m["dx"], m["dy"], odr=rodr, **kw)
+        assert equal_values(a, b), op
+        assert not equal_values(a, st), op
+
+
+@needs_ref
+@pytest.mark.parametrize("tables", MRX_TABLES)
+@pytest.mark.parametrize("kd", (0.1, 3.0, 30.0))
+@pytest.mark.parametrize("rodr", (2, 4))
+def test_conduction_matches_reference(port, rodr, kd, tables):
+    """Anisotropic heat conduction against the reference's t_conduction, at
+    diffusion numbers kd from a few to ~100 sweeps; with a periodic y axis the
+    reference's own mirror in y keeps the sweeps from converging, and both
+    run the 2048 sweeps of its CMAX (its abort is a no-op in the one-rank
+    stub)."""
+    from oracle import RefMRX
+
+    code = 5 if rodr == 2 else 4
+    st, m = ics.turbulence_2d(n=14, ny=10, seed=rodr + int(kd), odr=code, vrms=0.4)
+    rng = np.random.default_rng(7)
+    st["en"] = st["en"] * (1 + 0.1 * rng.uniform(-1, 1, st["en"].shape))
+    port.setbc2d(st, *tables)
+    dt = 0.3 * m["dx"] / m["vfast"]
+    kk0 = kd * m["dx"] ** 2 / dt
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    kw = dict(gamma=m["gamma"], dnx=tables[0], dny=tables[1])
+    n, err = port.conduction2d(a, kk0, dt, m["dx"], m["dy"], odr=code, **kw)
+    RefMRX.conduction2d(b, kk0, dt, m["dx"], m["dy"], odr=rodr, **kw)
+    assert equal_values(a, b)
+    assert not equal_values(a, st)
+    assert (err == -1) == (tables[1][0] == 0)
+    assert n == 2048 if err else 1 < n < 2048
 
 # reconstruction codes 1-4 (ODR) with every solver; 5, 6 (MUSCL with the MC /
 # Koren limiter, built by swapping calc_flr's limiter call) with two solvers
