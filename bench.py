@@ -421,6 +421,15 @@ def run_mrx2d(args):
                 fn(coef, dt)
             s.sync()
             op_ms[op] = (time.perf_counter() - t1) * 1e3 / args.steps
+        # heat conduction along B (off in the reference's MRX setup: kk0 = 0)
+        # at kk0 = eta0, with its Gauss-Seidel sweep count
+        sweeps = s.conduction(m["eta0"], dt)
+        s.sync()
+        t1 = time.perf_counter()
+        for _ in range(10):
+            sweeps = s.conduction(m["eta0"], dt)
+        op_ms["conduction"] = (time.perf_counter() - t1) * 1e3 / 10
+        op_ms["conduction_sweeps"] = sweeps
         launches = (s.launches_per_step + 3 * 4 + 1 + 3 * 3 + 3 + 1) * args.steps
     v = cells * args.steps / sec
     from oracle import Port

@@ -47,6 +47,13 @@ enum { MLAU_FLUX_MLAU = 0, MLAU_FLUX_LHLLD = 1, MLAU_FLUX_HLLD = 2, MLAU_FLUX_RO
 enum { MLAU_FP64 = 0, MLAU_FP32_SPLIT = 1 };
 /* 1D boundaries. */
 enum { MLAU_BC1D_OPEN = 0, MLAU_BC1D_PERIODIC = 1 };
+/* Eigen-system of the characteristic projection where the largest sonic
+ * Mach^2 of the face's three central cells is at least 1 (elsewhere the
+ * Alfven + entropy system): the drivers' full 7-wave system
+ * (mhd_c_reconst, mhd_eigen.h:455-530) or Miyoshi's fast + Alfven system
+ * (mhd_m_reconst, mhd_eigen.h:532-607), the header's alternative. */
+enum { MLAU_EIGEN_FULL = 0, MLAU_EIGEN_MIYOSHI = 1 };
+
 /* Output file formats (mlau_sim_outdat). */
 enum { MLAU_OUT_F64 = 0, MLAU_OUT_F32_RANK = 1 };
 
@@ -124,6 +131,10 @@ void t_conduction(const double *ro, const double *mx, const double *my, const do
  * 2D/MPI/MRX/mhd_fd_ct_2d.c:107) and the Koren limiter (interp.h:61-72), the
  * calc_flr alternatives the headers ship; everything else follows ODR 2. */
 int mlau_set_scheme(int dim, int odr, int flux, int nrk);
+/* Eigen-system of the drop-in drivers (MLAU_EIGEN_*; default full, or the
+ * environment variable MLAU_EIGEN=miyoshi at first use): the reference's
+ * driver with its mhd_c_reconst call replaced by mhd_m_reconst. */
+int mlau_set_eigen(int dim, int eig);
 int mlau_set_bc_1d(int bc);
 /* The boundary tables the drop-in drivers see: the problem program's own
  * dnxs / dnys / dnzs when it defines them (the library's weak all-zero
@@ -157,6 +168,8 @@ int mlau_sim_upload(mlau_sim *sim, const double *const *host8);
 int mlau_sim_download(mlau_sim *sim, double *const *host8);
 int mlau_sim_set_bx_1d(mlau_sim *sim, double bx);
 int mlau_sim_set_bc_1d(mlau_sim *sim, int bc);
+/* Eigen-system where Mach^2 >= 1 (MLAU_EIGEN_*; FP64 simulations). */
+int mlau_sim_set_eigen(mlau_sim *sim, int eig);
 /* Boundary tables of a 2D FP64 simulation: dnx[8] / dny[8] as the problem's
  * dnxs / dnys (2D/MPI/KHI/global.hpp:21-22; order ro mx my mz en bx by bz;
  * 0 periodic, -1 Dirichlet, +1 Neumann mirror), each array's ghosts filled by

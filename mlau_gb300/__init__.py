@@ -22,6 +22,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmlau_gb300.so")
 
 FLUX = {"mlau": 0, "lhlld": 1, "hlld": 2, "roe": 3}
+EIGEN = {"full": 0, "miyoshi": 1}
 FP64, FP32_SPLIT = 0, 1
 OUT_F64, OUT_F32_RANK = 0, 1
 BC1D = {"open": 0, "periodic": 1}
@@ -48,6 +49,8 @@ def _bind(lib):
     lib.mlau_sim_download.argtypes = [vp, C.POINTER(pd)]
     lib.mlau_sim_set_bx_1d.argtypes = [vp, d]
     lib.mlau_sim_set_bc_1d.argtypes = [vp, i]
+    lib.mlau_sim_set_eigen.argtypes = [vp, i]
+    lib.mlau_set_eigen.argtypes = [i, i]
     lib.mlau_sim_set_bc_2d.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
     lib.mlau_sim_step.argtypes = [vp, d, i]
     lib.mlau_sim_resistive_2d.argtypes = [vp, d, d]
@@ -150,6 +153,12 @@ def set_scheme(dim: int, odr: int, flux="lhlld", nrk: int = 3):
 
 def set_bc_1d(bc: str):
     _check(lib().mlau_set_bc_1d(BC1D[bc]))
+
+
+def set_eigen(dim: int, eig: str):
+    """Eigen-system of the drop-in drivers where Mach^2 >= 1 ("full" or
+    "miyoshi")."""
+    _check(lib().mlau_set_eigen(dim, EIGEN[eig]))
 
 
 def set_precision(dim: int, precision: int):
@@ -316,6 +325,11 @@ class Sim:
 
     def set_bc(self, bc: str):
         _check(lib().mlau_sim_set_bc_1d(self._h, BC1D[bc]))
+
+    def set_eigen(self, eig: str):
+        """Eigen-system where Mach^2 >= 1: "full" (the drivers') or
+        "miyoshi" (mhd_m_reconst)."""
+        _check(lib().mlau_sim_set_eigen(self._h, EIGEN[eig]))
 
     def set_bc2d(self, dnx, dny):
         """2D boundary tables (8 entries each, order ro mx my mz en bx by bz;

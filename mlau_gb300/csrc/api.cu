@@ -256,6 +256,21 @@ int mlau_sim_set_bc_2d(mlau_sim *s, const int *dnx, const int *dny)
     return MLAU_OK;
 }
 
+int mlau_sim_set_eigen(mlau_sim *s, int eig)
+{
+    if (!s || (eig != MLAU_EIGEN_FULL && eig != MLAU_EIGEN_MIYOSHI)) {
+        set_error("eigen-system must be MLAU_EIGEN_FULL or MLAU_EIGEN_MIYOSHI");
+        return MLAU_ERR_ARG;
+    }
+    if (s->precision != MLAU_FP64 && eig != MLAU_EIGEN_FULL) {
+        set_error("the Miyoshi eigen-system is built for the FP64 step only");
+        return MLAU_ERR_ARG;
+    }
+    if (s->eig != eig) drop_graph(s);
+    s->eig = eig;
+    return MLAU_OK;
+}
+
 int mlau_sim_set_bc_1d(mlau_sim *s, int bc)
 {
     if (!s || s->g.dim != 1 || (bc != MLAU_BC1D_OPEN && bc != MLAU_BC1D_PERIODIC)) {
@@ -448,7 +463,7 @@ int mlau_unpin_host(void *p)
 // ---------------------------------------------------------------------------
 namespace {
 
-struct Scheme { int odr, flux, nrk, precision; };
+struct Scheme { int odr, flux, nrk, precision, eig; };
 std::mutex g_mu;
 bool g_scheme_init = false;
 Scheme g_scheme[4];
@@ -468,14 +483,16 @@ int flux_from_name(const char *n)
 void init_scheme()
 {
     if (g_scheme_init) return;
-    g_scheme[3] = {2, MLAU_FLUX_LHLLD, 3, MLAU_FP64};
-    g_scheme[2] = {2, MLAU_FLUX_LHLLD, 3, MLAU_FP64};
-    g_scheme[1] = {1, MLAU_FLUX_LHLLD, 2, MLAU_FP64};
+    g_scheme[3] = {2, MLAU_FLUX_LHLLD, 3, MLAU_FP64, MLAU_EIGEN_FULL};
+    g_scheme[2] = {2, MLAU_FLUX_LHLLD, 3, MLAU_FP64, MLAU_EIGEN_FULL};
+    g_scheme[1] = {1, MLAU_FLUX_LHLLD, 2, MLAU_FP64, MLAU_EIGEN_FULL};
     const char *o = getenv("MLAU_ODR"), *r = getenv("MLAU_RK"), *f = getenv("MLAU_FLUX");
+    const char *e = getenv("MLAU_EIGEN");
     for (int d = 1; d <= 3; d++) {
         if (o) g_scheme[d].odr = atoi(o);
         if (r) g_scheme[d].nrk = atoi(r);
         if (f && flux_from_name(f) >= 0) g_scheme[d].flux = flux_from_name(f);
+        if (e && !strcmp(e, "miyoshi")) g_scheme[d].eig = MLAU_EIGEN_MIYOSHI;
     }
     g_scheme_init = true;
 }
@@ -511,6 +528,7 @@ mlau_sim *get_ctx(int dim, int nx, int ny, int nz, int ox, int oy, int oz, doubl
     if (c && c->g.nx == nx && c->g.ny == ny && c->g.nz == nz && c->g.ox == ox &&
         c->g.oy == oy && c->g.oz == oz && c->odr == sc.odr && c->flux == sc.flux &&
         c->nrk == sc.nrk && c->precision == sc.precision) {
+        if (c->eig != sc.eig && mlau_sim_set_eigen(c, sc.eig) != MLAU_OK) return nullptr;
         c->g.dx = dx;
         c->g.dy = dy;
         c->g.dz = dz;
@@ -521,6 +539,10 @@ mlau_sim *get_ctx(int dim, int nx, int ny, int nz, int ox, int oy, int oz, doubl
     if (mlau_sim_create(&c, dim, nx, ny, nz, ox, oy, oz, dx, dy, dz, gamma, sc.odr, sc.flux,
                         sc.nrk, sc.precision) != MLAU_OK)
         return nullptr;
+    if (mlau_sim_set_eigen(c, sc.eig) != MLAU_OK) {
+        mlau_sim_destroy(c);
+        return nullptr;
+    }
     g_ctx[dim] = c;
     return c;
 }
@@ -553,6 +575,18 @@ int mlau_set_scheme(int dim, int odr, int flux, int nrk)
     g_scheme[dim].odr = odr;
     g_scheme[dim].flux = flux;
     g_scheme[dim].nrk = nrk;
+    return MLAU_OK;
+}
+
+int mlau_set_eigen(int dim, int eig)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    init_scheme();
+    if (dim < 1 || dim > 3 || (eig != MLAU_EIGEN_FULL && eig != MLAU_EIGEN_MIYOSHI)) {
+        set_error("mlau_set_eigen: out of range");
+        return MLAU_ERR_ARG;
+    }
+    g_scheme[dim].eig = eig;
     return MLAU_OK;
 }
 

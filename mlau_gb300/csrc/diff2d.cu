@@ -437,11 +437,12 @@ k_cond_colour(Cond c, Dims d, CondCoef q, int py, int px, int nb, long long tota
 }
 
 // Block partial sums of res over [2, nx-2) x [2, ny-2): each thread strides
-// in a fixed order, then a fixed tree; deterministic for a geometry.
-__global__ void __launch_bounds__(kRedThreads) k_cond_sum(Cond c, Dims d, Box b)
+// in a fixed order, then a fixed tree; deterministic for a geometry.  In a
+// sweep (gated) it returns at once when the sweeps have stopped.
+__global__ void __launch_bounds__(kRedThreads) k_cond_sum(Cond c, Dims d, Box b, int gated)
 {
     __shared__ double sh[kRedThreads];
-    if (c.cb->st.done) return;
+    if (gated && c.cb->st.done) return;
     double acc = 0.0;
     const long long tot = (long long)b.e0 * b.e1 * b.e2;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
@@ -607,7 +608,7 @@ void enqueue_sweep(Sim *s, const Cond &c, const Dims &d, const CondCoef &q, cons
     }
     launch_fill(ft, d, st, &c.cb->st.done);
     const Box in{2, 2, 0, d.nx - 4, d.ny - 4, 1};
-    k_cond_sum<<<kRedBlocks, kRedThreads, 0, st>>>(c, d, in);
+    k_cond_sum<<<kRedBlocks, kRedThreads, 0, st>>>(c, d, in, 1);
     k_cond_check<<<1, kRedBlocks, 0, st>>>(c, 0, cmax);
 }
 
@@ -635,6 +636,8 @@ int diff2d_conduction(Sim *s, double kk0, double dt, int *sweeps)
         MLAU_CUDA(cudaMalloc(&s->d_cond, sizeof(CondBuf)));
         MLAU_CUDA(cudaMallocHost(&s->h_cond, sizeof(CondState)));
     }
+    // a fresh sweep state (the first reduction below then sets it up)
+    MLAU_CUDA(cudaMemsetAsync(s->d_cond, 0, sizeof(CondState), st));
     const Cond c{f.s[0], f.s[1], f.s[2], f.s[3], f.s[5], f.s[6], f.s[7], f.s[4],
                  f.ul[0], f.ul[1], f.ul[2], f.ul[3], f.ul[4], f.ul[5], f.ul[6], f.ur[0],
                  (CondBuf *)s->d_cond};
@@ -680,7 +683,7 @@ int diff2d_conduction(Sim *s, double kk0, double dt, int *sweeps)
     launch_fill(fe, d, st);
     k_cond_prep<<<blocks_for(g.n, TPB), TPB, 0, st>>>(c, g.n);
     k_cond_rhs<<<blocks_for(in.count(), TPB), TPB, 0, st>>>(c, d, in, q, dt);
-    k_cond_sum<<<kRedBlocks, kRedThreads, 0, st>>>(c, d, in);
+    k_cond_sum<<<kRedBlocks, kRedThreads, 0, st>>>(c, d, in, 0);
     k_cond_check<<<1, kRedBlocks, 0, st>>>(c, 1, cmax);
     MLAU_CUDA(cudaGetLastError());
     // the sweeps, kSweepChunk per graph launch, until the state says stop

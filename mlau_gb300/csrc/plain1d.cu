@@ -33,7 +33,7 @@ __global__ void k_prim1(PlainFields f, int nx, double bx, double gamma, int save
 
 // Face states (:133-186): full characteristic system where any of the three
 // central cells has sonic Mach^2 >= 1.
-__global__ void k_rec1(PlainFields f, int nx, int odr, double bx, double gamma)
+__global__ void k_rec1(PlainFields f, int nx, int odr, int eig, double bx, double gamma)
 {
     const int i = 2 + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx - 2) return;
@@ -58,8 +58,7 @@ __global__ void k_rec1(PlainFields f, int nx, int odr, double bx, double gamma)
         mach[t] = v2 / c2;
     }
     double ul[7], ur[7];
-    if (vmax(mach[0], vmax(mach[1], mach[2])) >= 1.0) reconst_full(odr, q, bx, gamma, ul, ur);
-    else reconst_alfven(odr, q, bx, gamma, ul, ur);
+    reconst_face(odr, eig, vmax(mach[0], vmax(mach[1], mach[2])), q, bx, gamma, ul, ur);
 #pragma unroll
     for (int n = 0; n < 7; n++) {
         f.ul[n][i + 1] = ul[n];
@@ -206,7 +205,7 @@ int plain1d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_REC);
-            k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, s->odr, s->bx1d, s->gamma);
+            k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, s->odr, s->eig, s->bx1d, s->gamma);
         }
         {
             TimedLaunch tl(&s->timer, KK_FLUX);
@@ -242,7 +241,7 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
         double ra, rb;
         rk_coef(nrk, rk, ra, rb);
         k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma, rk == 0);
-        k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, odr, bx, gamma);
+        k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, odr, EIG_FULL, bx, gamma);
         k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
         if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<2, 1, 0, st>>>(f, nx, off, bx, dtdx, gamma);
         k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(f, nx, off, odr, ra, rb, dtdx,

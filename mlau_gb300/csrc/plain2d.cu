@@ -77,7 +77,7 @@ View2 make_view2(const PlainFields &f, int D)
 }
 
 __global__ void __launch_bounds__(TPB)
-k_rec2(PlainFields f, View2 v, Dims d, Box b, long long st, int odr, double gamma)
+k_rec2(PlainFields f, View2 v, Dims d, Box b, long long st, int odr, int eig, double gamma)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
@@ -95,10 +95,8 @@ k_rec2(PlainFields f, View2 v, Dims d, Box b, long long st, int odr, double gamm
         q[6][m] = f.pr[s];
     }
     double ul[7], ur[7];
-    if (vmax(f.m2[c - st], vmax(f.m2[c], f.m2[c + st])) >= 1.0)
-        reconst_full(odr, q, v.cn[c], gamma, ul, ur);
-    else
-        reconst_alfven(odr, q, v.cn[c], gamma, ul, ur);
+    reconst_face(odr, eig, vmax(f.m2[c - st], vmax(f.m2[c], f.m2[c + st])), q, v.cn[c], gamma,
+                 ul, ur);
 #pragma unroll
     for (int n = 0; n < 7; n++) {
         f.ul[n][c + st] = ul[n];
@@ -299,7 +297,7 @@ int plain2d_step(Sim *s, double dt)
             {
                 TimedLaunch tl(&s->timer, KK_REC);
                 k_rec2<<<blocks_for(rb_.count(), TPB), TPB, 0, st>>>(f, v, d, rb_, stride, s->odr,
-                                                                     s->gamma);
+                                                                     s->eig, s->gamma);
             }
             {
                 TimedLaunch tl(&s->timer, KK_FLUX);

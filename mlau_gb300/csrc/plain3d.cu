@@ -84,7 +84,7 @@ __host__ SweepView make_view(const PlainFields &f, int D)
 }
 
 __global__ void __launch_bounds__(TPB)
-k_rec3(PlainFields f, SweepView v, Dims d, Box b, long long st, int odr, double gamma)
+k_rec3(PlainFields f, SweepView v, Dims d, Box b, long long st, int odr, int eig, double gamma)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
@@ -102,10 +102,8 @@ k_rec3(PlainFields f, SweepView v, Dims d, Box b, long long st, int odr, double 
         q[6][m] = f.pr[s];
     }
     double ul[7], ur[7];
-    if (vmax(f.m2[c - st], vmax(f.m2[c], f.m2[c + st])) >= 1.0)
-        reconst_full(odr, q, v.cn[c], gamma, ul, ur);
-    else
-        reconst_alfven(odr, q, v.cn[c], gamma, ul, ur);
+    reconst_face(odr, eig, vmax(f.m2[c - st], vmax(f.m2[c], f.m2[c + st])), q, v.cn[c], gamma,
+                 ul, ur);
 #pragma unroll
     for (int n = 0; n < 7; n++) {
         f.ul[n][c + st] = ul[n];
@@ -308,7 +306,7 @@ int plain3d_step(Sim *s, double dt)
             {
                 TimedLaunch tl(&s->timer, KK_REC);
                 k_rec3<<<blocks_for(rb_.count(), TPB), TPB, 0, st>>>(f, v, d, rb_, strides[D],
-                                                                     s->odr, s->gamma);
+                                                                     s->odr, s->eig, s->gamma);
             }
             {
                 TimedLaunch tl(&s->timer, KK_FLUX);

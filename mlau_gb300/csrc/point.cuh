@@ -424,6 +424,82 @@ MLAU_HD void reconst_full(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur
     zero_guard(q, ul, ur);
 }
 
+// Fast + Alfven projection of Miyoshi (mhd_m_reconst with mhd_eigen_mi,
+// mhd_eigen.h:194-324, 532-607; the slow mode is ignored), the header's
+// alternative to the full system.  The reference multiplies the dense 7x7
+// rows, zeros included, in index order; so does this (the zero products
+// decide signed zeros), with its rows written out.
+template <class T>
+MLAU_HD void reconst_miyoshi(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+{
+    const T ro = q[0][2], by = q[4][2], bz = q[5][2], pr = q[6][2];
+    const T iro = T(1.0) / ro;
+    const T cs2 = gamma * pr * iro;
+    const T ca2 = bn * bn * iro;
+    const T ct2 = (by * by + bz * bz) * iro;
+    const T cb2 = cs2 + ca2 + ct2;
+    const T cf2 = T(0.5) * (cb2 + tsqrt(tabs(cb2 * cb2 - T(4.0) * cs2 * ca2)));
+    const T cf = tsqrt(cf2);
+    const T rcf = ro * cf;
+    const T sro = tsqrt(ro);
+    const T isroh = T(0.5) / sro;
+    const T icf2 = T(1.0) / cf2;
+    const T icf2h = T(0.5) * icf2;
+    const T ircfh = T(0.5) / rcf;
+    const T byh = T(0.5) * by, bzh = T(0.5) * bz;
+    const T z = T(0), one = T(1.0);
+    // left rows l[n][k] and right columns r[k][n] of the reference
+    const T L[7][7] = {{z, -rcf, z, z, +by, +bz, +one},
+                       {cf2, z, z, z, -by, -bz, -one},
+                       {z, +rcf, z, z, +by, +bz, +one},
+                       {z, z, +sro, z, +one, z, z},
+                       {z, z, +sro, z, -one, z, z},
+                       {z, z, z, +sro, z, +one, z},
+                       {z, z, z, +sro, z, -one, z}};
+    const T R[7][7] = {{+icf2h, -ircfh, z, z, z, z, T(0.5)},
+                       {+icf2, z, z, z, z, z, z},
+                       {+icf2h, +ircfh, z, z, z, z, T(0.5)},
+                       {z, z, +isroh, z, T(0.5), z, -byh},
+                       {z, z, +isroh, z, T(-0.5), z, +byh},
+                       {z, z, z, +isroh, z, T(0.5), -bzh},
+                       {z, z, z, +isroh, z, T(-0.5), +bzh}};
+    T w[7][5];
+#pragma unroll
+    for (int n = 0; n < 7; n++)
+#pragma unroll
+        for (int m = 0; m < 5; m++)
+            w[n][m] = (+L[n][0] * q[0][m] + L[n][1] * q[1][m] + L[n][2] * q[2][m]
+                       + L[n][3] * q[3][m] + L[n][4] * q[4][m] + L[n][5] * q[5][m]
+                       + L[n][6] * q[6][m]);
+    T wl[7], wr[7];
+#pragma unroll
+    for (int n = 0; n < 7; n++) rec_lr(odr, w[n], wl[n], wr[n]);
+#pragma unroll
+    for (int n = 0; n < 7; n++) {
+        ul[n] = R[0][n] * wl[0] + R[1][n] * wl[1] + R[2][n] * wl[2] + R[3][n] * wl[3]
+                + R[4][n] * wl[4] + R[5][n] * wl[5] + R[6][n] * wl[6];
+        ur[n] = R[0][n] * wr[0] + R[1][n] * wr[1] + R[2][n] * wr[2] + R[3][n] * wr[3]
+                + R[4][n] * wr[4] + R[5][n] * wr[5] + R[6][n] * wr[6];
+    }
+    zero_guard(q, ul, ur);
+}
+
+// The eigen-system of a face: the full system (or Miyoshi's, eig = 1) where
+// the largest sonic Mach^2 of the three central cells is at least 1, the
+// Alfven + entropy system elsewhere (mhd_fd_ct_3d.c:416-420).
+enum { EIG_FULL = 0, EIG_MIYOSHI = 1 };
+template <class T>
+MLAU_HD void reconst_face(int odr, int eig, T mach2, const T q[7][5], T bn, T gamma, T ul[7],
+                          T ur[7])
+{
+    if (mach2 >= T(1.0)) {
+        if (eig == EIG_MIYOSHI) reconst_miyoshi(odr, q, bn, gamma, ul, ur);
+        else reconst_full(odr, q, bn, gamma, ul, ur);
+    } else {
+        reconst_alfven(odr, q, bn, gamma, ul, ur);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Riemann solvers (include/mhd_flux.h).  l/r: (ro, vn, vt, vu, bt, bu, pr),
 // bn: face-normal B, dv[2]: shock sensor (MLAU, LHLLD).  f: (ro, mn, mt, mu,

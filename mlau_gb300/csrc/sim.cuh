@@ -32,6 +32,7 @@ struct Sim {
     Geometry g;
     double gamma;
     int odr, flux, nrk, precision;
+    int eig = 0;         // eigen-system where Mach^2 >= 1: 0 full 7-wave, 1 Miyoshi
     int bc1d = MLAU_BC1D_OPEN;
     double bx1d = 0.0;
     Bc2 bc2{};           // 2D boundary tables (all zero: periodic)

@@ -66,26 +66,46 @@ class Port:
             lib.oracle_rec_lr.argtypes = [i, _cdp, C.POINTER(d), C.POINTER(d)]
             lib.oracle_flux.argtypes = [i, _cdp, _cdp, _dp]
             lib.oracle_reconst.argtypes = [i, i, _cdp, d, d, _dp, _dp]
+            lib.oracle_set_eigen.argtypes = [i]
+            lib.oracle_set_eigen.restype = None
             cls._lib = lib
         return cls._lib
 
     @classmethod
-    def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3):
+    def _eig(cls, eig):
+        """Context: the eigen-system ("full" or "miyoshi") for one call."""
+        lib = cls.lib()
+
+        class _Ctx:
+            def __enter__(self):
+                lib.oracle_set_eigen(1 if eig == "miyoshi" else 0)
+
+            def __exit__(self, *a):
+                lib.oracle_set_eigen(0)
+        return _Ctx()
+
+    @classmethod
+    def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3,
+               eig="full"):
         nz, ny, nx = s["ro"].shape
-        cls.lib().oracle_fd_ct_3d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
-                                  dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma, odr,
-                                  _flux_id(flux), nrk)
+        with cls._eig(eig):
+            cls.lib().oracle_fd_ct_3d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by",
+                                                       "bz")],
+                                      dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma, odr,
+                                      _flux_id(flux), nrk)
 
     @classmethod
     def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3, dnx=None,
-               dny=None):
+               dny=None, eig="full"):
         """dnx/dny: the problem's boundary tables (8 ints, order ro mx my mz en
         bx by bz; 0 periodic, -1 Dirichlet, +1 Neumann); None is periodic."""
         ny, nx = s["ro"].shape
         tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
-        cls.lib().oracle_fd_ct_2d_bc(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
-                                     dt, dx, dy, nx, ny, off, off, gamma, odr, _flux_id(flux), nrk,
-                                     tab(dnx), tab(dny))
+        with cls._eig(eig):
+            cls.lib().oracle_fd_ct_2d_bc(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by",
+                                                          "bz")],
+                                         dt, dx, dy, nx, ny, off, off, gamma, odr, _flux_id(flux),
+                                         nrk, tab(dnx), tab(dny))
 
     @classmethod
     def resistive2d(cls, s, eta0, dt, dx, dy, off=4, gamma=5 / 3, odr=2, nrk=3, dnx=None, dny=None):
@@ -127,11 +147,13 @@ class Port:
                                     nx, ny, off, off, tab(dnx), tab(dny))
 
     @classmethod
-    def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open"):
+    def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open",
+               eig="full"):
         nx = s["ro"].shape[0]
-        cls.lib().oracle_fd4c_1d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")],
-                                 bx, dt, dx, nx, off, gamma, odr, _flux_id(flux), nrk,
-                                 0 if bc == "open" else 1)
+        with cls._eig(eig):
+            cls.lib().oracle_fd4c_1d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")],
+                                     bx, dt, dx, nx, off, gamma, odr, _flux_id(flux), nrk,
+                                     0 if bc == "open" else 1)
 
     @classmethod
     def cfl3d(cls, s, cfl, dr, vfast, dt_old, off=4, gamma=5 / 3):
@@ -174,10 +196,10 @@ class Ref:
         return build.reference_available()
 
     @classmethod
-    def _get(cls, dim, odr, flux, nrk, bc="open"):
-        key = (dim, odr, flux, nrk, bc if dim == 1 else "")
+    def _get(cls, dim, odr, flux, nrk, bc="open", eig="full"):
+        key = (dim, odr, flux, nrk, bc if dim == 1 else "", eig)
         if key not in cls._libs:
-            lib = C.CDLL(build.build_ref_variant(dim, odr, flux, nrk, bc))
+            lib = C.CDLL(build.build_ref_variant(dim, odr, flux, nrk, bc, eig == "miyoshi"))
             d, i = C.c_double, C.c_int
             if dim == 1:
                 lib.ref_step_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d]
@@ -189,19 +211,20 @@ class Ref:
         return cls._libs[key]
 
     @classmethod
-    def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3):
+    def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3,
+               eig="full"):
         nz, ny, nx = s["ro"].shape
-        cls._get(3, odr, _flux_id(flux), nrk).ref_step(
+        cls._get(3, odr, _flux_id(flux), nrk, eig=eig).ref_step(
             *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
             dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma)
 
     @classmethod
     def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3, dnx=None,
-               dny=None):
+               dny=None, eig="full"):
         """dnx/dny: boundary tables written into the build's dnxs/dnys
         globals (global.hpp) for this call; None is periodic."""
         ny, nx = s["ro"].shape
-        lib = cls._get(2, odr, _flux_id(flux), nrk)
+        lib = cls._get(2, odr, _flux_id(flux), nrk, eig=eig)
         gx = (C.c_int * 8).in_dll(lib, "dnxs")
         gy = (C.c_int * 8).in_dll(lib, "dnys")
         for g, t in ((gx, dnx), (gy, dny)):
@@ -216,9 +239,10 @@ class Ref:
                     g[v] = 0
 
     @classmethod
-    def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open"):
+    def step1d(cls, s, bx, dt, dx, off=4, gamma=2.0, odr=2, flux="mlau", nrk=3, bc="open",
+               eig="full"):
         nx = s["ro"].shape[0]
-        cls._get(1, odr, _flux_id(flux), nrk, bc).ref_step_1d(
+        cls._get(1, odr, _flux_id(flux), nrk, bc, eig).ref_step_1d(
             *[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")], bx, dt, dx, nx, off, gamma)
 
 

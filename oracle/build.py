@@ -55,8 +55,9 @@ def reference_available() -> bool:
     return os.path.isfile(os.path.join(REF_ROOT, "include", "mhd_flux.h"))
 
 
-def _variant_name(dim: int, odr: int, flux: int, nrk: int, bc: str) -> str:
-    return f"ref{dim}d_o{odr}_{FLUX_NAMES[flux]}_rk{nrk}" + (f"_{bc}" if dim == 1 else "")
+def _variant_name(dim: int, odr: int, flux: int, nrk: int, bc: str, miyoshi: bool = False) -> str:
+    return (f"ref{dim}d_o{odr}_{FLUX_NAMES[flux]}_rk{nrk}" + (f"_{bc}" if dim == 1 else "")
+            + ("_mi" if miyoshi else ""))
 
 
 # reconstruction codes 5 and 6: ODR 2 with calc_flr's MUSCL limiter swapped
@@ -64,7 +65,12 @@ def _variant_name(dim: int, odr: int, flux: int, nrk: int, bc: str) -> str:
 LIMITER_SWAP = {5: "muscl_mc_cal_flr", 6: "muscl_kr_cal_flr"}
 
 
-def _patch_driver(text: str, odr: int, flux: int, nrk: int) -> str:
+def _patch_driver(text: str, odr: int, flux: int, nrk: int, miyoshi: bool = False) -> str:
+    if miyoshi:
+        # the header's alternative eigen-system where the driver uses the full one
+        text, nm = re.subn(r"\bmhd_c_reconst\(", "mhd_m_reconst(", text)
+        if nm < 1:
+            raise RuntimeError("reference driver layout not recognised; eigen patch failed")
     if odr in LIMITER_SWAP:
         text, n0 = re.subn(r"^(\s*)muscl_mm_cal_flr\(f\[1\],f\[2\],f\[3\],fl,fr\);",
                            lambda m: f"{m.group(1)}{LIMITER_SWAP[odr]}(f[1],f[2],f[3],fl,fr);",
@@ -83,7 +89,7 @@ def _patch_driver(text: str, odr: int, flux: int, nrk: int) -> str:
 
 
 def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
-                      bc: str = "open") -> str:
+                      bc: str = "open", miyoshi: bool = False) -> str:
     """Compile one scheme variant of the reference driver; return the .so path.
 
     dim 3: 3D/MPI/OTvortex/{mhd_fd_ct_3d.c,boundary.c}
@@ -93,7 +99,7 @@ def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
     """
     if not reference_available():
         raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
-    name = _variant_name(dim, odr, flux, nrk, bc)
+    name = _variant_name(dim, odr, flux, nrk, bc, miyoshi)
     out = os.path.join(REF_OUT, f"lib{name}.so")
     if os.path.exists(out):
         return out
@@ -108,7 +114,7 @@ def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
     src_dir = os.path.join(REF_OUT, "src", name)
     os.makedirs(src_dir, exist_ok=True)
     with open(os.path.join(REF_ROOT, d, drv)) as fh:
-        patched = _patch_driver(fh.read(), odr, flux, nrk)
+        patched = _patch_driver(fh.read(), odr, flux, nrk, miyoshi)
     drv_copy = os.path.join(src_dir, drv.replace(".c", ".cpp"))
     with open(drv_copy, "w") as fh:
         fh.write(patched)
@@ -190,6 +196,12 @@ def all_variants():
                 yield dict(dim=1, odr=odr, flux=flux, nrk=3, bc=bc)
         for odr in (5, 6):
             yield dict(dim=1, odr=odr, flux=0, nrk=3, bc=bc)
+    # Miyoshi's eigen-system swapped in where the drivers use the full one
+    for dim in (3, 2):
+        for odr, flux in ((4, 0), (4, 1), (2, 1), (3, 2)):
+            yield dict(dim=dim, odr=odr, flux=flux, nrk=3, miyoshi=True)
+    for odr, flux in ((2, 0), (4, 2)):
+        yield dict(dim=1, odr=odr, flux=flux, nrk=3, bc="open", miyoshi=True)
 
 
 def build_ref_all(jobs: int = 8) -> list:

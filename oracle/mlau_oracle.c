@@ -15,6 +15,12 @@
 #include "mlau_oracle.h"
 #include "oracle_point.h"
 
+/* Eigen-system where the drivers use the full one: 1 (mhd_c_reconst, the
+   drivers' choice) or 2 (Miyoshi's mhd_m_reconst swapped in). */
+static int o_full = 1;
+
+void oracle_set_eigen(int miyoshi) { o_full = miyoshi ? 2 : 1; }
+
 /* Phase hook of the op-counting build (oracle/opcount.cpp); no-op here.
  * 0 cell B + primitives, 1 CT weights + shock sensors, 2 reconstruction,
  * 3 Riemann flux, 4 edge EMF, 5 RK update + CT curl. */
@@ -142,7 +148,7 @@ static void sweep_pencil(const sweep_in *S, long base, long st, int len, int odr
             q[6][m] = S->pr[s];
         }
         double vl[7], vr[7];
-        int full = (o_max(S->m2[c - st], o_max(S->m2[c], S->m2[c + st])) >= 1.0);
+        int full = (o_max(S->m2[c - st], o_max(S->m2[c], S->m2[c + st])) >= 1.0) ? o_full : 0;
         o_reconst(full, odr, q, S->cn[c], gamma, vl, vr);
         for (int v = 0; v < 7; v++) {
             ul[7 * (i + 1) + v] = vl[v];
@@ -785,7 +791,7 @@ void oracle_fd4c_1d(double *ro, double *mx, double *my, double *mz, double *en, 
                             + q[3][1 + t] * q[3][1 + t];
                 mach[t] = v2 / c2;
             }
-            int full = (o_max(mach[0], o_max(mach[1], mach[2])) >= 1.0);
+            int full = (o_max(mach[0], o_max(mach[1], mach[2])) >= 1.0) ? o_full : 0;
             double vl[7], vr[7];
             o_reconst(full, odr, q, bx, gamma, vl, vr);
             for (int v = 0; v < 7; v++) {

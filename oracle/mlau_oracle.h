@@ -108,6 +108,10 @@ void oracle_ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, 
                           double nu0, double dt, double dx, double dy, int nx, int ny, int xoff,
                           int yoff, double gamma, int odr, int nrk, const int *dnx,
                           const int *dny);
+/* Eigen-system of the oracle's steps where Mach^2 >= 1: 0 the drivers' full
+ * 7-wave system, 1 Miyoshi's (the driver with mhd_c_reconst swapped for
+ * mhd_m_reconst). */
+void oracle_set_eigen(int miyoshi);
 /* Anisotropic heat conduction along B (t_conduction with diffusion2d_ani,
  * 2D/MPI/MRX/mhd_fd_ct_2d.c:1176-1456): implicit Crank-Nicolson in p/rho by
  * six-colour Gauss-Seidel; returns the sweep count, *err = -1 when cmax

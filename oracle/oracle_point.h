@@ -249,6 +249,41 @@ static void o_eigen_full(double ro, double vx, double vy, double vz, double bx, 
     }
 }
 
+/* mhd_eigen_mi, include/mhd_eigen.h:194-324 (Miyoshi's fast + Alfven
+ * projection; the slow mode is ignored). */
+static void o_eigen_miyoshi(double ro, double bx, double by, double bz, double pr,
+                            double gamma, double L[7][7], double R[7][7])
+{
+    double iro = 1.0 / ro;
+    double cs2 = gamma * pr * iro;
+    double ca2 = bx * bx * iro;
+    double ct2 = (by * by + bz * bz) * iro;
+    double cb2 = cs2 + ca2 + ct2;
+    double cf2 = 0.5 * (cb2 + sqrt(fabs(cb2 * cb2 - 4.0 * cs2 * ca2)));
+    double cf = sqrt(cf2);
+    double rcf = ro * cf, sro = sqrt(ro), isroh = 0.5 / sro;
+    double icf2 = 1.0 / cf2, icf2h = 0.5 * icf2, ircfh = 0.5 / rcf;
+    double byh = 0.5 * by, bzh = 0.5 * bz;
+    const double Lt[7][7] = {
+        {0, -rcf, 0, 0, +by, +bz, +1.0},
+        {cf2, 0, 0, 0, -by, -bz, -1.0},
+        {0, +rcf, 0, 0, +by, +bz, +1.0},
+        {0, 0, +sro, 0, +1.0, 0, 0},
+        {0, 0, +sro, 0, -1.0, 0, 0},
+        {0, 0, 0, +sro, 0, +1.0, 0},
+        {0, 0, 0, +sro, 0, -1.0, 0}};
+    const double Rt[7][7] = {
+        {+icf2h, -ircfh, 0, 0, 0, 0, +0.5},
+        {+icf2, 0, 0, 0, 0, 0, 0},
+        {+icf2h, +ircfh, 0, 0, 0, 0, +0.5},
+        {0, 0, +isroh, 0, +0.5, 0, -byh},
+        {0, 0, +isroh, 0, -0.5, 0, +byh},
+        {0, 0, 0, +isroh, 0, +0.5, -bzh},
+        {0, 0, 0, +isroh, 0, -0.5, +bzh}};
+    for (int n = 0; n < 7; n++)
+        for (int k = 0; k < 7; k++) { L[n][k] = Lt[n][k]; R[n][k] = Rt[n][k]; }
+}
+
 /* mhd_eigen_ae, include/mhd_eigen.h:326-453 (Alfven + entropy projection). */
 static void o_eigen_alfven(double ro, double bx, double by, double bz, double pr,
                            double gamma, double L[7][7], double R[7][7])
@@ -283,15 +318,18 @@ static void o_eigen_alfven(double ro, double bx, double by, double bz, double pr
         for (int k = 0; k < 7; k++) { L[n][k] = Lt[n][k]; R[n][k] = Rt[n][k]; }
 }
 
-/* mhd_c_reconst / mhd_a_reconst (include/mhd_eigen.h:455-530, 609-684):
- * project the 5-point stencil on characteristic fields, reconstruct each
- * field, project back, and keep identically-zero v and B at zero.
+/* mhd_c_reconst / mhd_a_reconst / mhd_m_reconst (include/mhd_eigen.h:455-530,
+ * 609-684, 532-607): project the 5-point stencil on characteristic fields,
+ * reconstruct each field, project back, and keep identically-zero v and B at
+ * zero.  full: 0 Alfven + entropy, 1 full 7-wave, 2 Miyoshi.
  * q[k][m]: variable k at stencil point m; ul at i+1/2, ur at i-1/2. */
 static void o_reconst(int full, int odr, const double q[7][5], double bn, double gamma,
                       double ul[7], double ur[7])
 {
     double L[7][7], R[7][7], lam[7];
-    if (full)
+    if (full == 2)
+        o_eigen_miyoshi(q[0][2], bn, q[4][2], q[5][2], q[6][2], gamma, L, R);
+    else if (full)
         o_eigen_full(q[0][2], q[1][2], q[2][2], q[3][2], bn, q[4][2], q[5][2], q[6][2],
                      gamma, lam, L, R);
     else

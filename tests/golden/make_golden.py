@@ -34,6 +34,9 @@ CASES_3D = [  # (name, n, mach, odr, flux, seed)
     ("3d_mlau_o4_lowmach", 8, 1e-2, 4, "mlau", 7),
     ("3d_mlau_o5", 8, 0.9, 5, "mlau", 8),
     ("3d_lhlld_o6", 8, 0.9, 6, "lhlld", 9),
+    # Miyoshi's eigen-system swapped in for the full one (names ending _mi)
+    ("3d_mlau_o4_mi", 8, 1.2, 4, "mlau", 10),
+    ("3d_hlld_o3_mi", 8, 1.2, 3, "hlld", 11),
 ]
 CASES_2D = [
     ("2d_lhlld_o4", 16, 4, "lhlld", 1),
@@ -43,6 +46,7 @@ CASES_2D = [
     ("2d_lhlld_o1", 16, 1, "lhlld", 5),
     ("2d_lhlld_o5", 16, 5, "lhlld", 6),
     ("2d_mlau_o6", 16, 6, "mlau", 7),
+    ("2d_lhlld_o4_mi", 16, 4, "lhlld", 8),
 ]
 CASES_1D = [  # (name, n, odr, flux, bc, seed)
     ("1d_mlau_o2_open", 64, 2, "mlau", "open", 1),
@@ -52,6 +56,7 @@ CASES_1D = [  # (name, n, odr, flux, bc, seed)
     ("1d_mlau_o4_periodic", 64, 4, "mlau", "periodic", 5),
     ("1d_mlau_o5_open", 64, 5, "mlau", "open", 6),
     ("1d_lhlld_o6_periodic", 64, 6, "lhlld", "periodic", 7),
+    ("1d_mlau_o2_open_mi", 64, 2, "mlau", "open", 8),
 ]
 # 2D with non-periodic boundary tables (the problem's dnxs / dnys), whole
 # arrays stored: (name, n, odr, flux, seed, dnx, dny); the initial ghosts are
@@ -96,13 +101,16 @@ def main(only=()):
         st, m = ics.turbulence_3d(n=n, mach=mach, seed=seed, odr=odr)
         dt = 0.3 * m["dx"] / m["vfast"]
         out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "odr": odr, "flux": flux}
+        eig = "miyoshi" if name.endswith("_mi") else "full"
+        if eig != "full":
+            out["eig"] = eig
         for k, v in st.items():
             out["in_" + k] = interior(v, 3)
         s = ics.copy_state(st)
         done = 0
         for nstep in STEPS:
             for _ in range(nstep - done):
-                Ref.step3d(s, dt, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux)
+                Ref.step3d(s, dt, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux, eig=eig)
             done = nstep
             for k, v in s.items():
                 out[f"out{nstep}_" + k] = interior(v, 3)
@@ -113,13 +121,16 @@ def main(only=()):
         st, m = ics.turbulence_2d(n=n, seed=seed, odr=odr, vrms=1.2)
         dt = 0.3 * m["dx"] / m["vfast"]
         out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "odr": odr, "flux": flux}
+        eig = "miyoshi" if name.endswith("_mi") else "full"
+        if eig != "full":
+            out["eig"] = eig
         for k, v in st.items():
             out["in_" + k] = interior(v, 2)
         s = ics.copy_state(st)
         done = 0
         for nstep in STEPS:
             for _ in range(nstep - done):
-                Ref.step2d(s, dt, m["dx"], m["dy"], odr=odr, flux=flux)
+                Ref.step2d(s, dt, m["dx"], m["dy"], odr=odr, flux=flux, eig=eig)
             done = nstep
             for k, v in s.items():
                 out[f"out{nstep}_" + k] = interior(v, 2)
@@ -152,13 +163,17 @@ def main(only=()):
         dt = Port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
         out = {"dt": dt, "dx": m["dx"], "gamma": m["gamma"], "bx": m["bx"], "odr": odr,
                "flux": flux, "bc": bc}
+        eig = "miyoshi" if name.endswith("_mi") else "full"
+        if eig != "full":
+            out["eig"] = eig
         for k, v in st.items():
             out["in_" + k] = v.copy()
         s = ics.copy_state(st)
         done = 0
         for nstep in STEPS:
             for _ in range(nstep - done):
-                Ref.step1d(s, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux, bc=bc)
+                Ref.step1d(s, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux, bc=bc,
+                           eig=eig)
             done = nstep
             for k, v in s.items():
                 out[f"out{nstep}_" + k] = v.copy()

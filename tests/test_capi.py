@@ -48,7 +48,8 @@ def test_cxx_linkage_drivers_exported(gpu_lib):
                     "_Z12mhd_fd_ct_2dPdS_S_S_S_S_S_S_dddiiiidiii",
                     "_Z11mhd_fd4c_1dPdS_S_S_S_S_S_dddiid",
                     "_Z14diff_ctfield_ePdS_S_S_ddddiiiidiii",
-                    "_Z13ns_viscous_2dPKdPdS1_S1_S1_ddddiiiidiii"):
+                    "_Z13ns_viscous_2dPKdPdS1_S1_S1_ddddiiiidiii",
+                    "_Z12t_conductionPKdS0_S0_S0_PdS0_S0_S0_ddddiiiidiii"):
         assert mangled in syms
 
 
@@ -96,3 +97,17 @@ def test_problem_boundary_tables_reach_the_library(tmp_path):
     assert list(got[:, 0]) == [0] * 8
     assert list(got[:, 1]) == [1, 1, -1, 1, 1, 1, -1, 1]
     assert list(got[:, 2]) == [0] * 8
+
+
+@pytest.mark.parametrize("prog", ("khi_dropin.c", "mrx_dropin.cpp"))
+def test_problem_programs_link(gpu_lib, tmp_path, prog):
+    """Programs in the shape of the reference's problems (their tables, the
+    reference's prototypes, C or C++ linkage) link against the library
+    alone: every driver symbol they use resolves (running them needs a GPU)."""
+    src = os.path.join(ROOT, "tests", "c", prog)
+    libdir = os.path.dirname(gpu_lib.LIB_PATH)
+    cc = "g++" if prog.endswith(".cpp") else "gcc"
+    r = subprocess.run([cc, "-O1", src, "-o", str(tmp_path / "a.out"), f"-L{libdir}",
+                        "-lmlau_gb300", f"-Wl,-rpath,{libdir}", "-Wl,--no-undefined"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -294,3 +294,42 @@ def test_conduction_full_size_vs_oracle(port):
         n = s.conduction(kk0, m3["dt"])
         got = s.download()
     assert err == 0 and n == n_ref and equal_values(got, ref)
+
+
+def test_mrx_problem_program_relinks(port, tmp_path):
+    """A C++ program in the shape of MRX's main.cpp (its tables, the
+    reference's prototypes with C++ linkage) links against the library in
+    place of the driver file and gives the oracle's results for 3 loops of
+    step + resistive diffusion + viscosity + heat conduction."""
+    import os
+    import subprocess
+
+    st, m = ics.mrx_2d(n=96, ny=48, lx=24, seed=4)
+    port.setbc2d(st, *ics.MRX_TABLES)
+    rng = np.random.default_rng(4)
+    st["en"] = st["en"] * (1 + 0.05 * rng.uniform(-1, 1, st["en"].shape))
+    ny, nx = st["ro"].shape
+    order = ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")
+    np.concatenate([st[k].ravel() for k in order]).tofile(tmp_path / "in.bin")
+    dt, eta0, nu0 = m["dt"], 0.05 * m["dx"] ** 2 / m["dt"], 0.04 * m["dx"] ** 2 / m["dt"]
+    kk0 = 1.0 * m["dx"] ** 2 / m["dt"]
+    src = os.path.join(os.path.dirname(__file__), "c", "mrx_dropin.cpp")
+    exe = tmp_path / "mrx_dropin"
+    libdir = os.path.dirname(M.LIB_PATH)
+    subprocess.run(["g++", "-O1", src, "-o", str(exe), f"-L{libdir}", "-lmlau_gb300",
+                    f"-Wl,-rpath,{libdir}"], check=True)
+    args = [repr(v) for v in (dt, m["dx"], m["dy"], m["gamma"], eta0, nu0, kk0)]
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), str(nx),
+                    str(ny), *args, "3"], check=True)
+    raw = np.fromfile(tmp_path / "out.bin")
+    got = {k: raw[i * nx * ny:(i + 1) * nx * ny].reshape(ny, nx) for i, k in enumerate(order)}
+    ref = ics.copy_state(st)
+    kw = dict(gamma=m["gamma"], odr=5, dnx=ics.MRX_TABLES[0], dny=ics.MRX_TABLES[1])
+    for _ in range(3):
+        port.step2d(ref, dt, m["dx"], m["dy"], flux="lhlld", nrk=3, **kw)
+        port.resistive2d(ref, eta0, dt, m["dx"], m["dy"], nrk=3, **kw)
+        port.viscous2d(ref, nu0, dt, m["dx"], m["dy"], nrk=3, **kw)
+        n, err = port.conduction2d(ref, kk0, dt, m["dx"], m["dy"], **kw)
+        assert err == 0
+    assert equal_values(got, ref), max_rel_diff(got, ref)
+

@@ -21,7 +21,9 @@ def gpu_run(dim, st, steps, dt, **kw):
     bx = kw.pop("bx", None)
     bc = kw.pop("bc", None)
     tables = kw.pop("tables", None)
+    eig = kw.pop("eig", "full")
     with M.Sim(dim, st["ro"].shape, **kw) as s:
+        s.set_eigen(eig)
         if bx is not None:
             s.set_bx(bx)
         if bc is not None:
@@ -39,7 +41,8 @@ def test_golden_3d(name):
     prm, s, outs = load_golden(name)
     for n, ref in outs.items():
         got = gpu_run(3, s, n, prm["dt"], dx=prm["dx"], dy=prm["dx"], dz=prm["dx"],
-                      gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"])
+                      gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"],
+                      eig=prm.get("eig", "full"))
         assert equal_values(got, ref), f"{name} after {n} steps: {max_rel_diff(got, ref)}"
 
 
@@ -49,7 +52,8 @@ def test_golden_2d(name):
     for n, ref in outs.items():
         tables = (prm["dnx"], prm["dny"]) if "dnx" in prm else None
         got = gpu_run(2, s, n, prm["dt"], dx=prm["dx"], dy=prm.get("dy", prm["dx"]),
-                      gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"], tables=tables)
+                      gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"], tables=tables,
+                      eig=prm.get("eig", "full"))
         assert equal_values(got, ref), f"{name} after {n} steps: {max_rel_diff(got, ref)}"
 
 
@@ -58,7 +62,7 @@ def test_golden_1d(name):
     prm, s, outs = load_golden(name)
     for n, ref in outs.items():
         got = gpu_run(1, s, n, prm["dt"], dx=prm["dx"], gamma=prm["gamma"], odr=prm["odr"],
-                      flux=prm["flux"], bx=prm["bx"], bc=prm["bc"])
+                      flux=prm["flux"], bx=prm["bx"], bc=prm["bc"], eig=prm.get("eig", "full"))
         assert equal_values(got, ref, keys=ref.keys()), f"{name} after {n} steps"
 
 
@@ -270,3 +274,46 @@ def test_dropin_2d_and_1d(port):
     M.mhd_fd4c_1d(*[st[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")], m["bx"], dt,
                   m["dx"], st["ro"].shape[0], 4, m["gamma"])
     assert equal_values(st, ref)
+
+
+@pytest.mark.parametrize("odr,flux", list(itertools.product(ORDERS, FLUXES)))
+def test_miyoshi_vs_oracle(port, odr, flux):
+    """Miyoshi's eigen-system (the headers' mhd_m_reconst) where the drivers
+    use the full one, 3D, 2D and 1D, supersonic states; the oracle is pinned
+    to the reference built with the call swapped in."""
+    st, m = ics.turbulence_3d(n=10, ny=9, nz=8, mach=1.2, seed=odr * 5 + len(flux), odr=odr)
+    ref = ics.copy_state(st)
+    for _ in range(2):
+        port.step3d(ref, 1e-3, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux, eig="miyoshi")
+    got = gpu_run(3, st, 2, 1e-3, dx=m["dx"], dy=m["dy"], dz=m["dz"], odr=odr, flux=flux,
+                  eig="miyoshi")
+    assert equal_values(got, ref, equal_nan=(flux == "roe")), max_rel_diff(got, ref)
+    st, m = ics.turbulence_2d(n=24, ny=18, seed=odr + 7, odr=odr, vrms=1.5)
+    ref = ics.copy_state(st)
+    for _ in range(3):
+        port.step2d(ref, 2e-3, m["dx"], m["dy"], odr=odr, flux=flux, eig="miyoshi")
+    got = gpu_run(2, st, 3, 2e-3, dx=m["dx"], dy=m["dy"], odr=odr, flux=flux, eig="miyoshi")
+    assert equal_values(got, ref, equal_nan=(flux == "roe")), max_rel_diff(got, ref)
+    st, m = ics.riemann_1d(n=64, seed=odr * 7 + len(flux))
+    v = st["mx"] / st["ro"]  # a uniform flow of 3 on top: supersonic cells
+    st["en"] = st["en"] + 0.5 * st["ro"] * ((v + 3.0) ** 2 - v ** 2)
+    st["mx"] = st["ro"] * (v + 3.0)
+    dt = port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
+    ref, full = ics.copy_state(st), ics.copy_state(st)
+    for _ in range(5):
+        port.step1d(ref, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux,
+                    eig="miyoshi")
+        port.step1d(full, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr, flux=flux)
+    assert not equal_values(ref, full, equal_nan=True)
+    got = gpu_run(1, st, 5, dt, dx=m["dx"], gamma=m["gamma"], odr=odr, flux=flux, bx=m["bx"],
+                  bc="open", eig="miyoshi")
+    assert equal_values(got, ref, keys=ref.keys(), equal_nan=(flux == "roe"))
+
+
+def test_miyoshi_refused_for_split():
+    st, m = ics.turbulence_3d(n=8, mach=0.5, seed=1)
+    with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"],
+               precision=M.FP32_SPLIT) as s:
+        with pytest.raises(M.MlauError, match="FP64"):
+            s.set_eigen("miyoshi")
+

@@ -17,7 +17,7 @@ def test_port_matches_golden_3d(port, name):
     for n in sorted(outs):
         for _ in range(n - done):
             port.step3d(s, prm["dt"], prm["dx"], prm["dx"], prm["dx"], gamma=prm["gamma"],
-                        odr=prm["odr"], flux=prm["flux"])
+                        odr=prm["odr"], flux=prm["flux"], eig=prm.get("eig", "full"))
         done = n
         assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
 
@@ -29,7 +29,8 @@ def test_port_matches_golden_2d(port, name):
     for n in sorted(outs):
         for _ in range(n - done):
             port.step2d(s, prm["dt"], prm["dx"], prm.get("dy", prm["dx"]), gamma=prm["gamma"],
-                        odr=prm["odr"], flux=prm["flux"], dnx=prm.get("dnx"), dny=prm.get("dny"))
+                        odr=prm["odr"], flux=prm["flux"], dnx=prm.get("dnx"), dny=prm.get("dny"),
+                        eig=prm.get("eig", "full"))
         done = n
         assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
 
@@ -41,7 +42,7 @@ def test_port_matches_golden_1d(port, name):
     for n in sorted(outs):
         for _ in range(n - done):
             port.step1d(s, prm["bx"], prm["dt"], prm["dx"], gamma=prm["gamma"], odr=prm["odr"],
-                        flux=prm["flux"], bc=prm["bc"])
+                        flux=prm["flux"], bc=prm["bc"], eig=prm.get("eig", "full"))
         done = n
         assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
 
@@ -232,3 +233,36 @@ def test_cfl_oracle_matches_formula(port):
     assert vmax > 0 and abs(dt - 0.4 * m["dx"] / vmax) < 1e-18
     dt2, vm2 = port.cfl3d(st, 0.4, m["dx"], 1e9, 1.0)
     assert vm2 == 1e9
+
+
+MIYOSHI = [(3, 4, "mlau"), (3, 4, "lhlld"), (3, 2, "lhlld"), (3, 3, "hlld"),
+           (2, 4, "mlau"), (2, 4, "lhlld"), (2, 2, "lhlld"), (2, 3, "hlld"),
+           (1, 2, "mlau"), (1, 4, "hlld")]
+
+
+@needs_ref
+@pytest.mark.parametrize("dim,odr,flux", MIYOSHI)
+def test_port_matches_reference_miyoshi(port, dim, odr, flux):
+    """Miyoshi's eigen-system (mhd_m_reconst) in place of the full one, against
+    the reference drivers built with that call swapped in; supersonic states
+    so that the full-system branch runs."""
+    if dim == 3:
+        st, m = ics.turbulence_3d(n=6, ny=7, nz=5, mach=1.2, seed=odr * 3 + len(flux), odr=odr)
+        run = lambda f, s, e: f.step3d(s, 1e-3, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux,
+                                       eig=e)
+    elif dim == 2:
+        st, m = ics.turbulence_2d(n=20, ny=14, seed=odr + 3, odr=odr, vrms=1.5)
+        run = lambda f, s, e: f.step2d(s, 2e-3, m["dx"], m["dy"], odr=odr, flux=flux, eig=e)
+    else:
+        st, m = ics.riemann_1d(n=48, seed=odr * 5)
+        dt = port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
+        run = lambda f, s, e: f.step1d(s, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=odr,
+                                       flux=flux, eig=e)
+    a, b, c = ics.copy_state(st), ics.copy_state(st), ics.copy_state(st)
+    for _ in range(6 if dim == 1 else 3):
+        run(port, a, "miyoshi")
+        run(Ref, b, "miyoshi")
+        run(port, c, "full")
+    assert equal_values(a, b)
+    assert not equal_values(a, c)
+
