@@ -189,6 +189,16 @@ int mlau_sim_viscous_2d(mlau_sim *sim, double nu0, double dt);
  * as the reference leaves it.  Synchronises the simulation's stream once per
  * 8 sweeps to test convergence. */
 int mlau_sim_conduction_2d(mlau_sim *sim, double kk0, double dt, int *sweeps);
+/* The RMI problem's inflow through the upper boundary (inj_ro,
+ * 2D/MPI/RMI/inj_ro.hpp:1-58, called before each step, main.cpp:48-54):
+ * rows [ny-yoff, ny) take density ro3 (+ dro3 (2u - 1) with noise[k] = u,
+ * the yoff*nx draws random()/RAND_MAX in row order, or no perturbation when
+ * noise is NULL), velocity (0, vy1 - vref, 0), B (bx1, by1, bz1) - By on the
+ * face row ny-yoff kept - and pressure pr1; then the main loop's periodic
+ * exchange of the 8 arrays along axes whose table entry 0 is zero.  2D FP64;
+ * noise is a host array, copied before the call returns. */
+int mlau_sim_inject_2d(mlau_sim *sim, double ro3, double dro3, double vy1, double bx1,
+                       double by1, double bz1, double pr1, double vref, const double *noise);
 /* nsteps full RK steps with fixed dt, enqueued on the simulation's stream. */
 int mlau_sim_step(mlau_sim *sim, double dt, int nsteps);
 /* CFL time step (3D/MPI/OTvortex/cflcheck.hpp:1-39, 2D cflcheck.hpp,

@@ -56,6 +56,7 @@ def _bind(lib):
     lib.mlau_sim_resistive_2d.argtypes = [vp, d, d]
     lib.mlau_sim_viscous_2d.argtypes = [vp, d, d]
     lib.mlau_sim_conduction_2d.argtypes = [vp, d, d, C.POINTER(i)]
+    lib.mlau_sim_inject_2d.argtypes = [vp] + [d] * 8 + [vp]
     lib.mlau_sim_cfl.argtypes = [vp, d, d, d, d, pd, pd]
     lib.mlau_sim_sync.argtypes = [vp]
     lib.mlau_sim_stream.argtypes = [vp]
@@ -247,7 +248,7 @@ class Sim:
             (ny, nx), nz = shape, 1
         else:
             (nx,), ny, nz = shape, 1, 1
-        self.dim, self.shape = dim, shape
+        self.dim, self.shape, self.off = dim, shape, off
         h = C.c_void_p()
         _check(lib().mlau_sim_create(C.byref(h), dim, nx, ny, nz, off, off if dim >= 2 else 0,
                                      off if dim == 3 else 0, dx, dy, dz, gamma, odr, _flux(flux),
@@ -348,6 +349,17 @@ class Sim:
     def viscous(self, nu0: float, dt: float):
         """Viscosity of the velocity (with the energy) over dt, 2D FP64."""
         _check(lib().mlau_sim_viscous_2d(self._h, nu0, dt))
+
+    def inject(self, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, noise=None):
+        """The RMI inflow at the upper boundary (inj_ro) and the periodic
+        exchange that follows it; noise: yoff*nx uniform draws or None."""
+        nz = None
+        if noise is not None:
+            nz = np.ascontiguousarray(noise, dtype=np.float64)
+            if nz.size < self.shape[-1] * self.off:
+                raise MlauError("noise needs yoff * nx draws")
+        _check(lib().mlau_sim_inject_2d(self._h, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref,
+                                        None if nz is None else nz.ctypes.data))
 
     def conduction(self, kk0: float, dt: float) -> int:
         """Anisotropic heat conduction along B over dt, 2D FP64; returns the

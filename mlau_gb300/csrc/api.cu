@@ -357,6 +357,13 @@ int mlau_sim_viscous_2d(mlau_sim *s, double nu0, double dt)
     return diff2d_viscous(s, nu0, dt);
 }
 
+int mlau_sim_inject_2d(mlau_sim *s, double ro3, double dro3, double vy1, double bx1, double by1,
+                       double bz1, double pr1, double vref, const double *noise)
+{
+    if (!s) { set_error("null simulation"); return MLAU_ERR_ARG; }
+    return diff2d_inject(s, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, noise);
+}
+
 int mlau_sim_conduction_2d(mlau_sim *s, double kk0, double dt, int *sweeps)
 {
     if (!s || !(dt == dt) || !(kk0 == kk0)) { set_error("bad arguments"); return MLAU_ERR_ARG; }

@@ -1,15 +1,19 @@
-// 2D MRX operators on the device (2D/MPI/MRX/mhd_fd_ct_2d.c:726-1174):
-// resistive diffusion of the CT field with uniform resistivity (diff_ctfield_e,
-// energy updated by the resistive Poynting flux) and the viscous term of the
-// Navier-Stokes equation with uniform kinematic viscosity (ns_viscous_2d).
-// Each is an explicit SSP-RK update of its own, run between hyperbolic steps
-// as the MRX problem's main loop does (2D/MPI/MRX/main.cpp:52-68).
+// 2D problem operators on the device, run between hyperbolic steps as the
+// problems' main loops do.
+//
+// MRX (2D/MPI/MRX/main.cpp:48-68, mhd_fd_ct_2d.c:726-1456): resistive
+// diffusion of the CT field with uniform resistivity (diff_ctfield_e, energy
+// updated by the resistive Poynting flux), the viscous term with uniform
+// kinematic viscosity (ns_viscous_2d) - explicit SSP-RK updates of their own -
+// and anisotropic heat conduction along B (t_conduction, implicit, solved by
+// colour Gauss-Seidel sweeps).  RMI (2D/MPI/RMI/main.cpp:48-54): the inflow
+// injected at the upper boundary before each step (inj_ro).
 //
 // Plain FP64, built with --fmad=false and the reference's evaluation order:
 // bit for bit the reference's results.  The boundary fills follow the MPI 2D
-// drivers' single-rank routines (periodic along an axis whose table entries
-// are zero, mirrors where they are +-1); tables must be all zero or all
-// nonzero per axis.  Scratch reuses the 2D step's arrays.
+// drivers' single-rank routines (periodic along an axis whose table entry 0
+// is zero, then mirrors where an entry is nonzero); tables must be all zero
+// or all nonzero per axis.  Scratch reuses the 2D step's arrays.
 #include "stencil.cuh"
 
 namespace mlau {
@@ -490,6 +494,39 @@ __global__ void __launch_bounds__(kRedBlocks) k_cond_check(Cond c, int first, in
     if (st.cnt == cmax) st.err = -1;
 }
 
+// ---- RMI inflow ------------------------------------------------------------------
+// inj_ro (2D/MPI/RMI/inj_ro.hpp:1-58): rows [ny-yoff, ny), every column, take
+// the upstream state; density ro_3 plus dro3 (2u - 1) with the draws u in loop
+// order (noise may be null); By on the face row j = ny-yoff keeps its value.
+struct Inflow {
+    double ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, gam;
+};
+
+__global__ void __launch_bounds__(TPB)
+k_inject2(PlainFields f, Dims d, Inflow q, const double *noise)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long cnt = (long long)d.oy * d.nx;
+    if (t >= cnt) return;
+    const int j = d.ny - d.oy + (int)(t / d.nx), i = (int)(t % d.nx);
+    const long long s = at2(d, i, j);
+    double ro = q.ro3;
+    if (noise) ro += q.dro3 * (noise[t] - 0.5) * 2.0;
+    const double vx = 0, vz = 0;
+    double vy = q.vy1;
+    vy -= q.vref;
+    const double bxc = q.bx1, byc = q.by1, bzc = q.bz1;
+    const double b2 = bxc * bxc + byc * byc + bzc * bzc;
+    f.s[0][s] = ro;
+    f.s[5][s] = bxc;
+    if (j != d.ny - d.oy) f.s[6][s] = q.by1;
+    f.s[7][s] = bzc;
+    f.s[1][s] = ro * vx;
+    f.s[2][s] = ro * vy;
+    f.s[3][s] = ro * vz;
+    f.s[4][s] = q.pr1 / (q.gam - 1) + 0.5 * (ro * (vx * vx + vy * vy + vz * vz) + b2);
+}
+
 int check_2d(Sim *s, const char *what)
 {
     if (s->g.dim != 2 || s->precision != MLAU_FP64) {
@@ -726,6 +763,41 @@ int diff2d_conduction(Sim *s, double kk0, double dt, int *sweeps)
         set_error("heat conduction did not converge within %d sweeps", cmax);
         return MLAU_ERR_CONVERGE;
     }
+    return MLAU_OK;
+}
+
+int diff2d_inject(Sim *s, double ro3, double dro3, double vy1, double bx1, double by1, double bz1,
+                  double pr1, double vref, const double *noise)
+{
+    if (s->g.dim != 2 || s->precision != MLAU_FP64) {
+        set_error("inflow injection: 2D FP64 simulations only");
+        return MLAU_ERR_ARG;
+    }
+    const Geometry &g = s->g;
+    PlainFields &f = s->f;
+    cudaStream_t st = s->stream;
+    const Dims d{g.nx, g.ny, 1, g.ox, g.oy, 0};
+    const long long cnt = (long long)g.oy * g.nx;
+    double *dn = nullptr;
+    if (noise) {
+        dn = f.ur[6];  // scratch of n >= cnt cells
+        MLAU_CUDA(cudaMemcpyAsync(dn, noise, sizeof(double) * cnt, cudaMemcpyHostToDevice, st));
+    }
+    const Inflow q{ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, s->gamma};
+    k_inject2<<<blocks_for(cnt, TPB), TPB, 0, st>>>(f, d, q, dn);
+    // the main loop's periodic exchange of the 8 arrays (RMI main.cpp:50-54)
+    for (int h = 0; h < 2; h++) {
+        Fill fl{};
+        fl.n = 4;
+        for (int v = 0; v < 4; v++) {
+            fl.a[v] = f.s[4 * h + v];
+            fl.x[v] = ax_of(s->bc2.x[0], 0, 0);
+            fl.y[v] = ax_of(s->bc2.y[0], 0, 0);
+        }
+        launch_fill(fl, d, st);
+    }
+    MLAU_CUDA(cudaGetLastError());
+    if (noise) MLAU_CUDA(cudaStreamSynchronize(st));  // the host draws may be reused at once
     return MLAU_OK;
 }
 

@@ -71,6 +71,8 @@ int split3d_check(Sim *s);
 int diff2d_resistive(Sim *s, double eta0, double dt);
 int diff2d_viscous(Sim *s, double nu0, double dt);
 int diff2d_conduction(Sim *s, double kk0, double dt, int *sweeps);
+int diff2d_inject(Sim *s, double ro3, double dro3, double vy1, double bx1, double by1, double bz1,
+                  double pr1, double vref, const double *noise);
 void diff2d_free(Sim *s);
 int cfl_compute(Sim *s, double *vmax_out);
 int launches_per_step(const Sim *s);

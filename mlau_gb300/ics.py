@@ -237,6 +237,72 @@ def mrx_2d(n=2048, ny=256, seed=0, off=4, gamma=5.0 / 3.0, lx=128.0, lam=1.0, be
                     dt=cfl * dr / vfast, eta0=lam / 5e2, nu0=lam / 5e2, tables=MRX_TABLES)
 
 
+def glibc_draws(seed, count):
+    """The C library's srandom(seed) then count draws of random()/RAND_MAX, as
+    doubles: the noise the reference's problems draw (RMI inflow,
+    2D/MPI/RMI/inj_ro.hpp:34-35), so that a run can reproduce it."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srandom.argtypes = [ctypes.c_uint]
+    libc.random.restype = ctypes.c_long
+    libc.srandom(seed)
+    rand_max = 2147483647.0
+    return np.array([float(libc.random()) / rand_max for _ in range(count)])
+
+
+def rmi_2d(n=128, ny=10240, off=4, gamma=5.0 / 3.0, ma_u=100.0, beta=1e5, vref=-0.625, psi=0.1,
+           ro_1=1.0, vy_1=-1.0, ro3_over_ro1=10.0, cfl=0.4):
+    """Richtmyer-Meshkov instability (2D/MPI/RMI/init.hpp:11-100,
+    global.hpp:11-80): a Mach-ma_u fast shock (jump conditions of the
+    reference) at y = 0 in the frame moving with vref, a contact of density
+    ro_3 = 10 ro_1 at y = 1 + psi cos(2 pi x), x periodic on [0, 1], y on
+    [-ly/2, ly/2] with Neumann walls and the upstream inflow injected at the
+    upper boundary before each step (`inflow`).  The single-mode interface of
+    the reference's default (RANDOM 0)."""
+    nx_, ny_ = n + 2 * off, ny + 2 * off
+    lx = 1.0
+    ly = lx * ny / n
+    dx, dy = lx / n, ly / ny
+    x = (np.arange(nx_) - off + 0.5) * dx
+    y = (np.arange(ny_) - off + 0.5) * dy - 0.5 * ly
+    pr_1 = (ro_1 * vy_1 * vy_1) / (gamma * ma_u * ma_u)
+    b0_1 = np.sqrt(2.0 * pr_1 / beta)
+    bx_1, by_1, bz_1 = b0_1, 0.0, 0.0
+    a = 2.0 * (2.0 - gamma) / beta
+    b = gamma * ((gamma - 1.0) * ma_u * ma_u + 2.0 / beta + 2.0)
+    c = -gamma * (gamma + 1.0) * ma_u * ma_u
+    r = (-b + np.sqrt(b * b - 4.0 * a * c)) / (2.0 * a)
+    rr = gamma * ma_u * ma_u * (1.0 - 1.0 / r) - (r * r - 1.0) / beta + 1.0
+    ro_2, vy_2, bx_2, bz_2, pr_2 = ro_1 * r, vy_1 / r, bx_1 * r, bz_1 * r, pr_1 * rr
+    ro_3 = ro_1 * ro3_over_ro1
+    dw = 0.5 * dy
+    ypos = 1.0 + psi * np.cos(2 * np.pi * x / lx)
+    X, Y = np.meshgrid(x, y)
+    sf = 0.5 * (1.0 + np.tanh(Y / dw))
+    ro = ro_2 + (ro_1 - ro_2) * sf
+    vy = vy_2 + (vy_1 - vy_2) * sf - vref
+    bx = bx_2 + (bx_1 - bx_2) * sf
+    by = np.full_like(ro, by_1)
+    bz = bz_2 + (bz_1 - bz_2) * sf
+    pr = pr_2 + (pr_1 - pr_2) * sf
+    ro = ro + (ro_3 - ro_1) * 0.5 * (1.0 + np.tanh((Y - ypos[None, :]) / dw))
+    b2 = bx * bx + by * by + bz * bz
+    z = np.zeros_like(ro)
+    st = {"ro": ro, "mx": z.copy(), "my": ro * vy, "mz": z.copy(),
+          "en": pr / (gamma - 1) + 0.5 * (ro * vy * vy + b2), "bx": bx, "by": by, "bz": bz}
+    st = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in st.items()}
+    vfast = float(np.sqrt((0.5 * gamma * 2.0 * pr_1 + b0_1 * b0_1) / ro_1))
+    inflow = dict(ro3=ro_3, dro3=0.1 * ro_3, vy1=vy_1, bx1=bx_1, by1=by_1, bz1=bz_1, pr1=pr_1,
+                  vref=vref)
+    # dt: the reference takes it from cflcheck before the loop (the flow at
+    # Mach 100 sets it, not vfast)
+    return st, dict(dx=dx, dy=dy, gamma=gamma, off=off, vfast=vfast, cfl=cfl, dr=min(dx, dy),
+                    tables=RMI_TABLES, inflow=inflow)
+
+
+RMI_TABLES = ((0,) * 8, (1,) * 8)  # 2D/MPI/RMI/global.hpp:21-22
+
+
 def riemann_1d(n=2048, seed=0, off=4, gamma=2.0):
     """Config-1 workload: seeded 1D Riemann problem on [0,1]; returns (state, meta)."""
     rng = np.random.default_rng(seed)

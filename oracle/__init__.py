@@ -68,6 +68,9 @@ class Port:
             lib.oracle_reconst.argtypes = [i, i, _cdp, d, d, _dp, _dp]
             lib.oracle_set_eigen.argtypes = [i]
             lib.oracle_set_eigen.restype = None
+            lib.oracle_inj_ro.argtypes = ([_dp] * 8 + [i] * 4 + [d] * 9
+                                          + [C.c_void_p, pi8, pi8])
+            lib.oracle_inj_ro.restype = None
             cls._lib = lib
         return cls._lib
 
@@ -136,6 +139,19 @@ class Port:
                                           kk0, dt, dx, dy, nx, ny, off, off, gamma, odr, tab(dnx),
                                           tab(dny), cmax, C.byref(err))
         return n, err.value
+
+    @classmethod
+    def inject2d(cls, s, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, gamma, noise=None, off=4,
+                 dnx=None, dny=None):
+        """inj_ro of the RMI problem plus its main loop's periodic exchange,
+        in place; noise: the uniform draws in loop order, or None."""
+        ny, nx = s["ro"].shape
+        tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
+        nz = None if noise is None else np.ascontiguousarray(noise, dtype=np.float64)
+        cls.lib().oracle_inj_ro(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                                nx, ny, off, off, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, gamma,
+                                None if nz is None else nz.ctypes.data_as(C.c_void_p), tab(dnx),
+                                tab(dny))
 
     @classmethod
     def setbc2d(cls, s, dnx, dny, off=4):
@@ -316,3 +332,30 @@ class RefMRX:
         cls._call(lib.ref_t_conduction, lib, dnx, dny,
                   *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
                   kk0, dt, dx, dy, nx, ny, off, off, gamma)
+
+
+class RefRMI:
+    """ctypes binding of the reference's RMI inflow routine (inj_ro.hpp)
+    built into oracle/_ref."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            lib = C.CDLL(build.build_ref_rmi())
+            d, i = C.c_double, C.c_int
+            lib.ref_inj_ro.argtypes = [_dp] * 8 + [i] * 4 + [d] * 9 + [C.c_uint]
+            lib.ref_inj_ro.restype = None
+            cls._lib = lib
+        return cls._lib
+
+    @classmethod
+    def inject2d(cls, s, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, gamma, seed=0, off=4):
+        """The routine alone (its random() draws from srandom(seed)); the
+        periodic exchange of the main loop is not part of it."""
+        ny, nx = s["ro"].shape
+        cls.lib().ref_inj_ro(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                             nx, ny, off, off, ro3, dro3, vy1, bx1, by1, bz1, pr1, vref, gamma,
+                             seed)
+

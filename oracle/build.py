@@ -180,6 +180,24 @@ def build_ref_mrx(odr: int = 2, nrk: int = 3) -> str:
     return out
 
 
+def build_ref_rmi() -> str:
+    """Compile the reference's RMI inflow routine (2D/MPI/RMI/inj_ro.hpp) with
+    oracle/ref_rmi_harness.cpp; return the .so path."""
+    if not reference_available():
+        raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
+    out = os.path.join(REF_OUT, "libref_rmi.so")
+    harness = os.path.join(HERE, "ref_rmi_harness.cpp")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(harness):
+        return out
+    os.makedirs(REF_OUT, exist_ok=True)
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["g++", "-x", "c++", *CFLAGS, "-I" + os.path.join(REF_ROOT, "2D/MPI/RMI"),
+           "-I" + os.path.join(HERE, "ref_stub"), "-o", tmp, harness, "-lm"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+    os.replace(tmp, out)
+    return out
+
+
 def all_variants():
     for dim in (3, 2):
         for odr in (1, 2, 3, 4):

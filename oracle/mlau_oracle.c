@@ -1339,3 +1339,43 @@ int oracle_t_conduction(const double *ro, const double *mx, const double *my, co
     return cnt;
 }
 
+/* inj_ro (2D/MPI/RMI/inj_ro.hpp:1-58): the RMI problem's inflow through the
+   upper boundary, set before each step on the rows [ny-yoff, ny) of the top
+   rank: uniform upstream state (velocity vy_1 - vref), density ro_3 plus
+   dro3 * (2u - 1) with u the draws (double)random()/RAND_MAX in loop order
+   (noise, or none when NULL); By on the boundary face row j = ny-yoff keeps
+   its value (CT spacing).  Then the main loop's periodic exchange
+   (mpi_sdrv2d of the 8 arrays, main.cpp:50-54). */
+void oracle_inj_ro(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                   double *by, double *bz, int nx, int ny, int xoff, int yoff, double ro_3,
+                   double dro3, double vy_1, double bx_1, double by_1, double bz_1, double pr_1,
+                   double vref, double gam, const double *noise, const int *dnx_in,
+                   const int *dny_in)
+{
+    const int *dnx = dnx_in ? dnx_in : o_zero8, *dny = dny_in ? dny_in : o_zero8;
+    long k = 0;
+    for (int j = ny - yoff; j < ny; j++) {
+        const int ctyflg = (j == (ny - yoff));
+        for (int i = 0; i < nx; i++) {
+            const long ss = (long)nx * j + i;
+            ro[ss] = ro_3;
+            if (noise) ro[ss] += dro3 * (noise[k++] - 0.5) * 2.0;
+            double vx = 0, vy = vy_1, vz = 0;
+            vy -= vref;
+            double bxc, byc, bzc;
+            bx[ss] = bxc = bx_1;
+            by[ss] = ctyflg ? by[ss] : by_1;
+            byc = by_1;
+            bz[ss] = bzc = bz_1;
+            const double b2 = bxc * bxc + byc * byc + bzc * bzc;
+            const double pr = pr_1;
+            mx[ss] = ro[ss] * vx;
+            my[ss] = ro[ss] * vy;
+            mz[ss] = ro[ss] * vz;
+            en[ss] = pr / (gam - 1) + 0.5 * (ro[ss] * (vx * vx + vy * vy + vz * vz) + b2);
+        }
+    }
+    double *p[8] = {ro, mx, my, mz, en, bx, by, bz};
+    o_sdrv2d(p, 8, dnx[0], dny[0], nx, ny, xoff, yoff);
+}
+

@@ -108,6 +108,14 @@ void oracle_ns_viscous_2d(const double *ro, double *mx, double *my, double *mz, 
                           double nu0, double dt, double dx, double dy, int nx, int ny, int xoff,
                           int yoff, double gamma, int odr, int nrk, const int *dnx,
                           const int *dny);
+/* The RMI problem's inflow (inj_ro, 2D/MPI/RMI/inj_ro.hpp:1-58) and the
+ * periodic exchange its main loop runs after it; noise: the random() / RAND_MAX
+ * draws in loop order, or NULL. */
+void oracle_inj_ro(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                   double *by, double *bz, int nx, int ny, int xoff, int yoff, double ro_3,
+                   double dro3, double vy_1, double bx_1, double by_1, double bz_1, double pr_1,
+                   double vref, double gam, const double *noise, const int *dnx,
+                   const int *dny);
 /* Eigen-system of the oracle's steps where Mach^2 >= 1: 0 the drivers' full
  * 7-wave system, 1 Miyoshi's (the driver with mhd_c_reconst swapped for
  * mhd_m_reconst). */

@@ -85,6 +85,13 @@ CASES_MRX = [
     ("mrx2d_o4_rk3_cond_walls", 20, 24, 4, 4, 3, 26, WALLS, MRX_TABLES[1], 2.0),
 ]
 MRX_LOOPS = (1, 3)
+# The RMI problem's main loop (2D/MPI/RMI/main.cpp:46-58): the inflow at the
+# upper boundary (inj_ro, with its random() density perturbation drawn after
+# srandom(seed + loop)), the periodic exchange along x, the MPI 2D step (ODR 2,
+# LHLLD, RK3 - the serial driver with the same tables gives the same result);
+# whole arrays and the draws stored: (name, n, ny, seed)
+CASES_RMI = [("rmi2d_o2", 16, 48, 5)]
+RMI_LOOPS = (1, 3)
 STEPS = (1, 4)
 
 
@@ -206,6 +213,36 @@ def main(only=()):
                 RefMRX.viscous2d(s, nu0, dt, m["dx"], m["dy"], **kw)
                 if kk0 > 0:
                     RefMRX.conduction2d(s, kk0, dt, m["dx"], m["dy"], **kw)
+            done = nloop
+            for k, v in s.items():
+                out[f"out{nloop}_" + k] = v.copy()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, n, ny, seed in CASES_RMI:
+        if skip(name):
+            continue
+        from oracle import Port, RefRMI
+        st, m = ics.rmi_2d(n=n, ny=ny)
+        inf = m["inflow"]
+        dt, _ = Port.cfl2d(st, m["cfl"], m["dr"], m["vfast"], 0.0)
+        nx = st["ro"].shape[1]
+        draws = np.stack([ics.glibc_draws(seed + k, OFF * nx) for k in range(max(RMI_LOOPS))])
+        out = {"dim": 2, "dt": dt, "dx": m["dx"], "dy": m["dy"], "gamma": m["gamma"], "odr": 2,
+               "flux": "lhlld", "dnx": np.array(m["tables"][0]), "dny": np.array(m["tables"][1]),
+               "draws": draws, **{"inflow_" + k: v for k, v in inf.items()}}
+        for k, v in st.items():
+            out["in_" + k] = v.copy()
+        s = ics.copy_state(st)
+        done = 0
+        for nloop in RMI_LOOPS:
+            for k in range(done, nloop):
+                RefRMI.inject2d(s, inf["ro3"], inf["dro3"], inf["vy1"], inf["bx1"], inf["by1"],
+                                inf["bz1"], inf["pr1"], inf["vref"], m["gamma"], seed=seed + k)
+                for a in s.values():  # mpi_sdrv2d of one rank: x periodic
+                    for i in range(OFF):
+                        a[:, nx - 1 - i] = a[:, 2 * OFF - 1 - i]
+                        a[:, i] = a[:, nx - 2 * OFF + i]
+                Ref.step2d(s, dt, m["dx"], m["dy"], odr=2, flux="lhlld", dnx=m["tables"][0],
+                           dny=m["tables"][1])
             done = nloop
             for k, v in s.items():
                 out[f"out{nloop}_" + k] = v.copy()

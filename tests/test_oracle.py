@@ -266,3 +266,54 @@ def test_port_matches_reference_miyoshi(port, dim, odr, flux):
     assert equal_values(a, b)
     assert not equal_values(a, c)
 
+
+def run_rmi_loop(port, s, prm, k0, k1):
+    """The RMI problem's main loop (2D/MPI/RMI/main.cpp:46-58) on the oracle:
+    inflow with the stored draws, periodic exchange, step."""
+    tables = (prm["dnx"], prm["dny"])
+    for k in range(k0, k1):
+        port.inject2d(s, prm["inflow_ro3"], prm["inflow_dro3"], prm["inflow_vy1"],
+                      prm["inflow_bx1"], prm["inflow_by1"], prm["inflow_bz1"], prm["inflow_pr1"],
+                      prm["inflow_vref"], prm["gamma"], noise=prm["draws"][k], dnx=tables[0],
+                      dny=tables[1])
+        port.step2d(s, prm["dt"], prm["dx"], prm["dy"], gamma=prm["gamma"], odr=prm["odr"],
+                    flux=prm["flux"], dnx=tables[0], dny=tables[1])
+
+
+@pytest.mark.parametrize("name", golden_cases("rmi"))
+def test_port_matches_golden_rmi(port, name):
+    prm, s, outs = load_golden(name)
+    done = 0
+    for n in sorted(outs):
+        run_rmi_loop(port, s, prm, done, n)
+        done = n
+        assert equal_values(s, outs[n]), f"{name}: differs after {n} loops"
+
+
+@needs_ref
+@pytest.mark.parametrize("seed,perturb", [(0, False), (7, True), (123, True)])
+def test_inflow_matches_reference(port, seed, perturb):
+    """The RMI inflow against the reference's inj_ro (its random() draws after
+    srandom(seed)), followed on both sides by the periodic x exchange."""
+    from oracle import RefRMI
+
+    st, m = ics.rmi_2d(n=32, ny=64)
+    inf = m["inflow"]
+    rng = np.random.default_rng(seed)
+    for k in st:
+        st[k] = st[k] + rng.uniform(-1e-3, 1e-3, st[k].shape)
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    nx = st["ro"].shape[1]
+    dro3 = inf["dro3"] if perturb else 0.0
+    args = (inf["ro3"], dro3, inf["vy1"], inf["bx1"], inf["by1"], inf["bz1"], inf["pr1"],
+            inf["vref"], m["gamma"])
+    port.inject2d(a, *args, noise=ics.glibc_draws(seed, 4 * nx) if perturb else None,
+                  dnx=m["tables"][0], dny=m["tables"][1])
+    RefRMI.inject2d(b, *args, seed=seed)
+    for f in b.values():
+        for i in range(4):
+            f[:, nx - 1 - i] = f[:, 7 - i]
+            f[:, i] = f[:, nx - 8 + i]
+    assert equal_values(a, b)
+    assert not equal_values(a, st)
+
