@@ -21,9 +21,10 @@ stepping (captured graphs of `steps_per_tick` steps) and retirement happen
 there, between engine runs.  The HBM budget is divided between the lanes
 when the server starts; a request waits (FIFO per lane) until its lane has a
 slot and room for its cells.  The 1D and 2D lanes share the SMs through a
-block allocator: each takes a grid proportional to its live cells and the
-grids together never exceed what is co-resident, so the lanes' persistent
-kernels run side by side.  1D requests always run in FP64 (the 1D problem
+block allocator: the 1D lane (the smallest requests in work) takes the
+blocks it can use first, the 2D lanes split the rest in proportion to their
+live cells, and the grids together never exceed what is co-resident, so the
+lanes' persistent kernels run side by side.  1D requests always run in FP64 (the 1D problem
 is small; its FP64 step is cheap).
 """
 from __future__ import annotations
@@ -128,24 +129,43 @@ def make_requests(n, rate, seed=0, mix=(0.5, 0.4, 0.1), n1d=(256, 16384), n2d=(6
 class _Blocks:
     """Co-resident blocks shared by the lanes' persistent kernels.  A lane
     takes a grant before a run and gives it back after, so the grids running
-    at one time never add up to more than fit together."""
+    at one time never add up to more than fit together.
+
+    Priority lanes (the 1D lane: its requests are the smallest in work,
+    cells x steps, so serving them first is shortest-remaining-work-first)
+    are granted the blocks they can use - one per tile of their live
+    instances - first; the other lanes share the rest in proportion to their
+    live cells (their work per step)."""
 
     def __init__(self, total):
         self.total = total
         self.free = total
         self.load = {}
+        self.useful = {}
+        self.prio = set()
         self.cv = threading.Condition()
 
-    def set_load(self, lane, cells):
+    def set_load(self, lane, cells, useful=None, prio=False):
         with self.cv:
             self.load[lane] = cells
+            self.useful[lane] = useful
+            if prio:
+                self.prio.add(lane)
+
+    def _want(self, lane, floor):
+        if lane in self.prio:
+            u = self.useful.get(lane) or self.total
+            return min(max(floor, u), self.total // 2)
+        held = sum(min(max(floor, self.useful.get(p) or 0), self.total // 2)
+                   for p in self.prio if self.load.get(p, 0) > 0)
+        rest = max(self.total - held, floor)
+        busy = sum(v for k, v in self.load.items() if v > 0 and k not in self.prio)
+        share = rest * self.load.get(lane, 0) / max(busy, 1)
+        return min(max(floor, int(share) // floor * floor), self.total)
 
     def acquire(self, lane, floor=8):
         with self.cv:
-            busy = sum(v for v in self.load.values() if v > 0)
-            share = self.total * self.load.get(lane, 0) / max(busy, 1)
-            want = max(floor, int(share) // floor * floor)
-            want = min(want, self.total)
+            want = self._want(lane, floor)
             while self.free < min(want, floor):
                 self.cv.wait(0.05)
             got = min(want, self.free)
@@ -185,10 +205,11 @@ class _Lane(threading.Thread):
 
 
 class _BatchLane(_Lane):
-    def __init__(self, server, name, batch, steps_per_tick):
+    def __init__(self, server, name, batch, steps_per_tick, prio=False, tile=None):
         super().__init__(server, name)
         self.batch, self.k = batch, steps_per_tick
         self.live: dict[int, Request] = {}
+        self.prio, self.tile = prio, tile
 
     def _admit(self):
         while self.waiting:
@@ -217,7 +238,10 @@ class _BatchLane(_Lane):
         while not srv.abort.is_set():
             self._drain(block=not self.live)
             self._admit()
-            srv.blocks.set_load(self.lane, sum(r.interior for r in self.live.values()))
+            cells = sum(r.interior for r in self.live.values())
+            useful = (sum(-(-r.interior // self.tile) for r in self.live.values())
+                      if self.tile else None)
+            srv.blocks.set_load(self.lane, cells, useful, self.prio)
             if not self.live:
                 if srv.closing.is_set() and not self.waiting and self.inbox.empty():
                     return
@@ -343,7 +367,10 @@ class Server:
         self._wake = threading.Event()
         self._lock = threading.Lock()
         self.done: list[Request] = []
-        self.lanes = {k: _BatchLane(self, k, b, spt[k]) for k, b in self.batches.items()}
+        # the 1D lane is served first (see _Blocks); a block per 64-cell tile
+        self.lanes = {k: _BatchLane(self, k, b, spt[k], prio=(k == "1d"),
+                                    tile=64 if k == "1d" else None)
+                      for k, b in self.batches.items()}
         self.lanes["3d"] = _Lane3D(self, budget_bytes * shares["3d"])
         self.t0 = None
 
