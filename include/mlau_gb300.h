@@ -64,7 +64,8 @@ enum { MLAU_OUT_F64 = 0, MLAU_OUT_F32_RANK = 1 };
 /* Replaces mhd_fd_ct_3d (3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-103, prototype
  * 3D/MPI/OTvortex/myfunc.h:48-52, caller 3D/MPI/OTvortex/main.cpp:48-50).
  * Single GPU: mpi_numx = mpi_numy = mpi_numz = 1 and mpi_rank = 0 are
- * required. */
+ * required.  The problem's tables dnxs / dnys / dnzs apply (each axis all
+ * zero or all nonzero; non-periodic ones with the FP64 form). */
 void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
                   double *by, double *bz, double dt, double dx, double dy, double dz, int nx,
                   int ny, int nz, int xoff, int yoff, int zoff, double gamma, int mpi_rank,
@@ -168,6 +169,13 @@ int mlau_sim_upload(mlau_sim *sim, const double *const *host8);
 int mlau_sim_download(mlau_sim *sim, double *const *host8);
 int mlau_sim_set_bx_1d(mlau_sim *sim, double bx);
 int mlau_sim_set_bc_1d(mlau_sim *sim, int bc);
+/* Boundary tables of a 3D simulation (dnxs / dnys / dnzs of the problem,
+ * 3D/MPI/OTvortex/global.hpp:22-24; order ro mx my mz en bx by bz; 0
+ * periodic, -1 Dirichlet, +1 Neumann mirror as mpi_xbc3d / _ybc3d / _zbc3d,
+ * 3D/MPI/OTvortex/boundary.c:227-309, at the driver's three fill sites).
+ * Each axis's entries all zero or all nonzero; non-periodic tables need the
+ * FP64 form.  All zero (the default) is periodic. */
+int mlau_sim_set_bc_3d(mlau_sim *sim, const int *dnx, const int *dny, const int *dnz);
 /* Eigen-system where Mach^2 >= 1 (MLAU_EIGEN_*; FP64 simulations). */
 int mlau_sim_set_eigen(mlau_sim *sim, int eig);
 /* Boundary tables of a 2D FP64 simulation: dnx[8] / dny[8] as the problem's

@@ -52,6 +52,7 @@ def _bind(lib):
     lib.mlau_sim_set_eigen.argtypes = [vp, i]
     lib.mlau_set_eigen.argtypes = [i, i]
     lib.mlau_sim_set_bc_2d.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+    lib.mlau_sim_set_bc_3d.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
     lib.mlau_sim_step.argtypes = [vp, d, i]
     lib.mlau_sim_resistive_2d.argtypes = [vp, d, d]
     lib.mlau_sim_viscous_2d.argtypes = [vp, d, d]
@@ -331,6 +332,13 @@ class Sim:
         """Eigen-system where Mach^2 >= 1: "full" (the drivers') or
         "miyoshi" (mhd_m_reconst)."""
         _check(lib().mlau_sim_set_eigen(self._h, EIGEN[eig]))
+
+    def set_bc3d(self, dnx, dny, dnz):
+        """3D boundary tables (8 entries each, order ro mx my mz en bx by bz;
+        0 periodic, -1 Dirichlet, +1 Neumann; each axis all zero or all
+        nonzero)."""
+        t = [(C.c_int * 8)(*[int(v) for v in a]) for a in (dnx, dny, dnz)]
+        _check(lib().mlau_sim_set_bc_3d(self._h, *t))
 
     def set_bc2d(self, dnx, dny):
         """2D boundary tables (8 entries each, order ro mx my mz en bx by bz;

@@ -108,7 +108,7 @@ int launches_per_step(const Sim *s)
 {
     // kernels per RK stage (device-to-device copies are not counted)
     if (s->precision == MLAU_FP32_SPLIT) return s->nrk * 7;
-    if (s->g.dim == 3) return s->nrk * 10;
+    if (s->g.dim == 3) return s->nrk * (s->walls3d ? 12 : 10);
     if (s->g.dim == 2) return s->nrk * (s->walls2d ? 10 : 8);
     return s->nrk * 4 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
 }
@@ -253,6 +253,45 @@ int mlau_sim_set_bc_2d(mlau_sim *s, const int *dnx, const int *dny)
         s->bc2.y[v] = dny[v];
     }
     s->walls2d = walls;
+    return MLAU_OK;
+}
+
+int mlau_sim_set_bc_3d(mlau_sim *s, const int *dnx, const int *dny, const int *dnz)
+{
+    if (!s || s->g.dim != 3 || !dnx || !dny || !dnz) {
+        set_error("boundary tables of mlau_sim_set_bc_3d apply to 3D simulations");
+        return MLAU_ERR_ARG;
+    }
+    bool walls = false;
+    for (const int *t : {dnx, dny, dnz}) {
+        int nz = 0;
+        for (int v = 0; v < 8; v++) {
+            if (t[v] < -1 || t[v] > 1) {
+                set_error("boundary table entries are -1, 0 or +1");
+                return MLAU_ERR_ARG;
+            }
+            nz += t[v] != 0;
+        }
+        if (nz != 0 && nz != 8) {
+            set_error("3D tables: each axis's entries must be all zero or all nonzero (the MPI "
+                      "driver decides periodicity from entry 0)");
+            return MLAU_ERR_ARG;
+        }
+        walls = walls || nz != 0;
+    }
+    if (walls && s->precision != MLAU_FP64) {
+        set_error("non-periodic 3D boundaries are built for the FP64 step only");
+        return MLAU_ERR_ARG;
+    }
+    if (std::memcmp(s->bc3.x, dnx, sizeof(s->bc3.x)) || std::memcmp(s->bc3.y, dny, sizeof(s->bc3.y)) ||
+        std::memcmp(s->bc3.z, dnz, sizeof(s->bc3.z)))
+        drop_graph(s);
+    for (int v = 0; v < 8; v++) {
+        s->bc3.x[v] = dnx[v];
+        s->bc3.y[v] = dny[v];
+        s->bc3.z[v] = dnz[v];
+    }
+    s->walls3d = walls;
     return MLAU_OK;
 }
 
@@ -515,17 +554,6 @@ __attribute__((visibility("default"))) extern int dnys[8];
 __attribute__((visibility("default"))) extern int dnzs[8];
 }
 
-bool tables_periodic(int dim)
-{
-    int *t[3] = {dnxs, dnys, dnzs};
-    for (int d = 0; d < dim && d < 3; d++) {
-        if (!t[d]) continue;
-        for (int v = 0; v < 8; v++)
-            if (t[d][v] != 0) return false;
-    }
-    return true;
-}
-
 mlau_sim *get_ctx(int dim, int nx, int ny, int nz, int ox, int oy, int oz, double dx, double dy,
                   double dz, double gamma)
 {
@@ -650,14 +678,12 @@ void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, do
         report("mhd_fd_ct_3d");
         return;
     }
-    if (!tables_periodic(3)) {
-        set_error("only periodic boundaries (dnxs/dnys/dnzs all 0) are implemented");
-        report("mhd_fd_ct_3d");
-        return;
-    }
+    static const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int *tx = dnxs ? dnxs : zero, *ty = dnys ? dnys : zero, *tz = dnzs ? dnzs : zero;
     mlau_sim *c = get_ctx(3, nx, ny, nz, xoff, yoff, zoff, dx, dy, dz, gamma);
     double *h[8] = {ro, mx, my, mz, en, bx, by, bz};
-    if (!c || run_dropin(c, h, dt) != MLAU_OK) report("mhd_fd_ct_3d");
+    if (!c || mlau_sim_set_bc_3d(c, tx, ty, tz) != MLAU_OK || run_dropin(c, h, dt) != MLAU_OK)
+        report("mhd_fd_ct_3d");
 }
 
 // 2D drivers with the problem's dnxs/dnys.  The serial driver fills each

@@ -51,6 +51,11 @@ struct Bc2 {
     int x[8], y[8];
 };
 
+// Boundary tables of a 3D problem (dnxs/dnys/dnzs, same order).
+struct Bc3 {
+    int x[8], y[8], z[8];
+};
+
 // Kernel-kind identifiers for the optional per-kernel event timing.
 enum KernelKind {
     KK_PRIM = 0, KK_AUX, KK_REC, KK_FLUX, KK_EMF, KK_UPDATE, KK_COPY, KK_CFL,

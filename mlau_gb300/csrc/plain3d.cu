@@ -1,20 +1,29 @@
-// Plain FP64 3D step: one SSP-RK step of ideal MHD with constrained transport
-// on a periodic box, the GPU form of the reference driver
-// 3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-1198 (single rank).
+// Plain FP64 3D step: one SSP-RK step of ideal MHD with constrained transport,
+// the GPU form of the reference driver 3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-1198
+// (single rank), with the problem's boundary tables dnxs/dnys/dnzs: periodic
+// along an axis whose entries are zero, Dirichlet / Neumann mirrors
+// (3D/MPI/OTvortex/boundary.c:227-309) where they are -1 / +1.
 //
 // Compiled with --fmad=false: every floating-point expression is evaluated
 // as in the reference (same operands, same order, IEEE division and square
 // root), so the result equals the reference's bit for bit.
 //
 // Per RK stage, each kernel reads the reference's own index sets:
-//   prim     cell-centred B (periodic images of ghosts, :186-238) + primitives (:240-262)
-//   aux      CT upwind weights (:264-340) + shock sensors with periodic images (:342-377)
+//   prim     cell-centred B (ghosts at their boundary sources, :186-238) + primitives (:240-262)
+//   aux      CT upwind weights (:264-340) + shock sensors, ghosts at their sources (:342-377)
 //   rec<D>   characteristic reconstruction of each cell along axis D (:394-454)
 //   flux<D>  Riemann flux at each face along D, CT central/upwind split (:457-487)
 //   emf      edge EMFs ex, ey, ez from the face fluxes (:494-585, :702-793, :910-1001)
 //   update   RK combine of cell-centred variables (:1003-1078) and CT curl of
-//            face B (:1079-1157); each thread also writes its periodic ghost
-//            images, which is exactly the reference's periodic fill (:1161-1175).
+//            face B (:1079-1157); on a periodic box each thread also writes its
+//            periodic ghost images, which is exactly the reference's fill
+//            (:1161-1175); with walls, face + bc follow (the right boundary faces
+//            the CT loops reach, then the ghost fill with the tables).
+// A ghost's boundary source composes, axis by axis, the periodic image or the
+// mirror with the product of the signs: the result of the reference's
+// periodic exchange followed by its X, Y and Z mirrors.
+#include <algorithm>
+
 #include "sim.cuh"
 #include "point.cuh"
 #include "stencil.cuh"
@@ -22,17 +31,29 @@
 namespace mlau {
 namespace {
 
-__global__ void __launch_bounds__(TPB) k_prim3(PlainFields f, Dims d, Box b, int odr, double gamma)
+// Source of cell (i, j, k) of a cell-centred ghost-filled array whose x/y/z
+// table entries are dx/dy/dz (sign into *g).
+__device__ __forceinline__ long long src3(const Dims &d, int i, int j, int k, int dx, int dy,
+                                          int dz, double *g)
+{
+    return d.at(bc_src(i, d.nx, d.ox, 0, dx, g), bc_src(j, d.ny, d.oy, 0, dy, g),
+                bc_src(k, d.nz, d.oz, 0, dz, g));
+}
+
+__global__ void __launch_bounds__(TPB)
+k_prim3(PlainFields f, Dims d, Box b, int odr, double gamma, Bc3 bc)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
     const long long sy = d.nx, sz = (long long)d.nx * d.ny;
-    const int iw = wrap_idx(i, d.nx, d.ox), jw = wrap_idx(j, d.ny, d.oy), kw = wrap_idx(k, d.nz, d.oz);
-    const long long w = d.at(iw, jw, kw);
+    double gx = 1.0, gy = 1.0, gz = 1.0;
+    const long long wx = src3(d, i, j, k, bc.x[5], bc.y[5], bc.z[5], &gx);
+    const long long wy = src3(d, i, j, k, bc.x[6], bc.y[6], bc.z[6], &gy);
+    const long long wz = src3(d, i, j, k, bc.x[7], bc.y[7], bc.z[7], &gz);
     const double *bx = f.s[5], *by = f.s[6], *bz = f.s[7];
-    const double cx = face2cen(odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
-    const double cy = face2cen(odr, by[w - sy], by[w], by[w + sy], by[w + 2 * sy]);
-    const double cz = face2cen(odr, bz[w - sz], bz[w], bz[w + sz], bz[w + 2 * sz]);
+    const double cx = gx * face2cen(odr, bx[wx - 1], bx[wx], bx[wx + 1], bx[wx + 2]);
+    const double cy = gy * face2cen(odr, by[wy - sy], by[wy], by[wy + sy], by[wy + 2 * sy]);
+    const double cz = gz * face2cen(odr, bz[wz - sz], bz[wz], bz[wz + sz], bz[wz + 2 * sz]);
     const long long s = d.at(i, j, k);
     const double ro = f.s[0][s];
     const double iro = 1.0 / ro;
@@ -50,7 +71,10 @@ __global__ void __launch_bounds__(TPB) k_prim3(PlainFields f, Dims d, Box b, int
     f.cz[s] = cz;
 }
 
-__global__ void __launch_bounds__(TPB) k_aux3(PlainFields f, Dims d, Box b)
+// CT weights, and the shock sensors with the sign rules of their ghost fill
+// (:367-376): dvx takes -dnxs[1] along x, dvy -dnys[2] along y, dvz -dnzs[3]
+// along z, the table entries along the other axes.
+__global__ void __launch_bounds__(TPB) k_aux3(PlainFields f, Dims d, Box b, Bc3 bc)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
@@ -64,11 +88,13 @@ __global__ void __launch_bounds__(TPB) k_aux3(PlainFields f, Dims d, Box b)
                                     : 0.5;
     f.ct[2][s] = (k >= 1 && i >= 1) ? ct_weight(f.vz, f.vx, ro, f.s[7], f.s[5], s, sz, 1, 1, sz)
                                     : 0.5;
-    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy),
-                             wrap_idx(k, d.nz, d.oz));
-    f.dv[0][s] = vmin((f.vx[w + 1] - f.vx[w]), (f.vx[w] - f.vx[w - 1]));
-    f.dv[1][s] = vmin((f.vy[w + sy] - f.vy[w]), (f.vy[w] - f.vy[w - sy]));
-    f.dv[2][s] = vmin((f.vz[w + sz] - f.vz[w]), (f.vz[w] - f.vz[w - sz]));
+    double g0 = 1.0, g1 = 1.0, g2 = 1.0;
+    const long long w0 = src3(d, i, j, k, -bc.x[1], bc.y[1], bc.z[1], &g0);
+    const long long w1 = src3(d, i, j, k, bc.x[2], -bc.y[2], bc.z[2], &g1);
+    const long long w2 = src3(d, i, j, k, bc.x[3], bc.y[3], -bc.z[3], &g2);
+    f.dv[0][s] = g0 * vmin((f.vx[w0 + 1] - f.vx[w0]), (f.vx[w0] - f.vx[w0 - 1]));
+    f.dv[1][s] = g1 * vmin((f.vy[w1 + sy] - f.vy[w1]), (f.vy[w1] - f.vy[w1 - sy]));
+    f.dv[2][s] = g2 * vmin((f.vz[w2 + sz] - f.vz[w2]), (f.vz[w2] - f.vz[w2 - sz]));
 }
 
 // Rotated views of the primitives for a sweep along axis D.
@@ -193,7 +219,7 @@ __global__ void __launch_bounds__(TPB) k_emf3(PlainFields f, Dims d, Box b, int 
 
 __global__ void __launch_bounds__(TPB)
 k_update3(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dtdx, double dtdy,
-          double dtdz)
+          double dtdz, int images)
 {
     int i, j, k;
     if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
@@ -226,6 +252,11 @@ k_update3(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dt
         const double d1 = fdiff(odr, ex[s - sy], ex[s], ex[s + sy], ex[s + 2 * sy]);
         out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - dtdx * d0 + dtdy * d1);
     }
+    if (!images) {
+#pragma unroll
+        for (int v = 0; v < 8; v++) f.s[v][s] = out[v];
+        return;
+    }
     // periodic images: i+N for i < 2*off, i-N for i >= N (N interior width)
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
@@ -242,6 +273,60 @@ k_update3(PlainFields f, Dims d, Box b, int odr, double ra, double rb, double dt
                 for (int v = 0; v < 8; v++) f.s[v][t] = out[v];
             }
         }
+    }
+}
+
+// The right boundary faces the CT loops also update (:1079-1157 run one face
+// further: Bx at i = nx-xoff, By at j = ny-yoff, Bz at k = nz-zoff); they
+// survive the ghost fill only where that axis mirrors the face array.  One
+// thread per face of the three planes.
+__global__ void __launch_bounds__(TPB)
+k_face3(PlainFields f, Dims d, int odr, double ra, double rb, double dtdx, double dtdy,
+        double dtdz, int do_x, int do_y, int do_z)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long sy = d.nx, sz = (long long)d.nx * d.ny;
+    const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
+    const double *ex = f.e[0], *ey = f.e[1], *ez = f.e[2];
+    if (do_x && t < (long long)Ny * Nz) {  // Bx at i = nx - xoff
+        const long long s = d.at(d.nx - d.ox, d.oy + (int)(t % Ny), d.oz + (int)(t / Ny));
+        const double d0 = fdiff(odr, ez[s - sy], ez[s], ez[s + sy], ez[s + 2 * sy]);
+        const double d1 = fdiff(odr, ey[s - sz], ey[s], ey[s + sz], ey[s + 2 * sz]);
+        f.s[5][s] = ra * f.u0[5][s] + rb * (f.s[5][s] - dtdy * d0 + dtdz * d1);
+    }
+    if (do_y && t < (long long)Nx * Nz) {  // By at j = ny - yoff
+        const long long s = d.at(d.ox + (int)(t % Nx), d.ny - d.oy, d.oz + (int)(t / Nx));
+        const double d0 = fdiff(odr, ex[s - sz], ex[s], ex[s + sz], ex[s + 2 * sz]);
+        const double d1 = fdiff(odr, ez[s - 1], ez[s], ez[s + 1], ez[s + 2]);
+        f.s[6][s] = ra * f.u0[6][s] + rb * (f.s[6][s] - dtdz * d0 + dtdx * d1);
+    }
+    if (do_z && t < (long long)Nx * Ny) {  // Bz at k = nz - zoff
+        const long long s = d.at(d.ox + (int)(t % Nx), d.oy + (int)(t / Nx), d.nz - d.oz);
+        const double d0 = fdiff(odr, ey[s - 1], ey[s], ey[s + 1], ey[s + 2]);
+        const double d1 = fdiff(odr, ex[s - sy], ex[s], ex[s + sy], ex[s + 2 * sy]);
+        f.s[7][s] = ra * f.u0[7][s] + rb * (f.s[7][s] - dtdx * d0 + dtdy * d1);
+    }
+}
+
+// Ghost fill of the conserved arrays with the tables (:1161-1175): each
+// ghost takes its boundary source composed over the three axes, times the
+// signs.  Sources are interior cells or computed faces.
+__global__ void __launch_bounds__(TPB) k_bc3(PlainFields f, Dims d, Box b, Bc3 bc)
+{
+    int i, j, k;
+    if (!b.decode((long long)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+    if (i >= d.ox && i < d.nx - d.ox && j >= d.oy && j < d.ny - d.oy && k >= d.oz &&
+        k < d.nz - d.oz)
+        return;
+    const long long s = d.at(i, j, k);
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+        double g = 1.0;
+        const int si = bc_src(i, d.nx, d.ox, v == 5, bc.x[v], &g);
+        const int sj = bc_src(j, d.ny, d.oy, v == 6, bc.y[v], &g);
+        const int sk = bc_src(k, d.nz, d.oz, v == 7, bc.z[v], &g);
+        if (si == i && sj == j && sk == k) continue;
+        f.s[v][s] = g * f.s[v][d.at(si, sj, sk)];
     }
 }
 
@@ -287,11 +372,12 @@ int plain3d_step(Sim *s, double dt)
         rk_coef(s->nrk, rk, ra, rb);
         {
             TimedLaunch tl(&s->timer, KK_PRIM);
-            k_prim3<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->odr, s->gamma);
+            k_prim3<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->odr, s->gamma,
+                                                                  s->bc3);
         }
         {
             TimedLaunch tl(&s->timer, KK_AUX);
-            k_aux3<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all);
+            k_aux3<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->bc3);
         }
         for (int D = 0; D < 3; D++) {
             const SweepView v = make_view(f, D);
@@ -321,7 +407,15 @@ int plain3d_step(Sim *s, double dt)
         {
             TimedLaunch tl(&s->timer, KK_UPDATE);
             k_update3<<<blocks_for(inner.count(), TPB), TPB, 0, st>>>(f, d, inner, s->odr, ra, rb,
-                                                                      dtdx, dtdy, dtdz);
+                                                                      dtdx, dtdy, dtdz, !s->walls3d);
+            if (s->walls3d) {
+                const long long n = std::max({(long long)g.ny * g.nz, (long long)g.nx * g.nz,
+                                              (long long)g.nx * g.ny});
+                k_face3<<<blocks_for(n, TPB), TPB, 0, st>>>(f, d, s->odr, ra, rb, dtdx, dtdy, dtdz,
+                                                            s->bc3.x[5] != 0, s->bc3.y[6] != 0,
+                                                            s->bc3.z[7] != 0);
+                k_bc3<<<blocks_for(all.count(), TPB), TPB, 0, st>>>(f, d, all, s->bc3);
+            }
         }
         MLAU_CUDA(cudaGetLastError());
     }

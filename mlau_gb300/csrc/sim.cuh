@@ -37,6 +37,8 @@ struct Sim {
     double bx1d = 0.0;
     Bc2 bc2{};           // 2D boundary tables (all zero: periodic)
     bool walls2d = false;  // some 2D table entry is not periodic
+    Bc3 bc3{};           // 3D boundary tables (all zero: periodic)
+    bool walls3d = false;  // some 3D table entry is not periodic
     cudaStream_t stream = nullptr;
     PlainFields f{};
     SplitFields *sp = nullptr;

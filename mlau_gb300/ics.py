@@ -334,8 +334,9 @@ def copy_state(s):
     return {k: v.copy() for k, v in s.items()}
 
 
-def div_b_3d(st, dx, dy, dz, off=4, odr=4):
-    """max |div B| * dx / max|B| over interior cells with the scheme difference."""
+def div_b_3d(st, dx, dy, dz, off=4, odr=4, base=None):
+    """max |div B| * dx / max|B| over interior cells with the scheme
+    difference; with `base`, the change of div B from that state."""
     def d(f, ax, h):
         f1 = f
         f2 = np.roll(f, -1, axis=ax)
@@ -344,6 +345,8 @@ def div_b_3d(st, dx, dy, dz, off=4, odr=4):
         f0, f3 = np.roll(f, 1, axis=ax), np.roll(f, -2, axis=ax)
         return (27.0 * (f2 - f1) - (f3 - f0)) / 24.0 / h
     div = d(st["bx"], 2, dx) + d(st["by"], 1, dy) + d(st["bz"], 0, dz)
+    if base is not None:
+        div = div - (d(base["bx"], 2, dx) + d(base["by"], 1, dy) + d(base["bz"], 0, dz))
     sl = (slice(off, -off),) * 3
     bmax = max(np.abs(st[k][sl]).max() for k in ("bx", "by", "bz"))
     return float(np.abs(div[sl]).max() * min(dx, dy, dz) / bmax)

@@ -40,6 +40,9 @@ class Port:
             d, i = C.c_double, C.c_int
             lib.oracle_fd_ct_3d.argtypes = [_dp] * 8 + [d, d, d, d] + [i] * 6 + [d, i, i, i]
             lib.oracle_fd_ct_3d.restype = None
+            lib.oracle_fd_ct_3d_bc.argtypes = ([_dp] * 8 + [d, d, d, d] + [i] * 6 + [d, i, i, i]
+                                               + [C.POINTER(C.c_int)] * 3)
+            lib.oracle_fd_ct_3d_bc.restype = None
             lib.oracle_fd_ct_2d.argtypes = [_dp] * 8 + [d, d, d] + [i] * 4 + [d, i, i, i]
             lib.oracle_fd_ct_2d.restype = None
             pi8 = C.POINTER(C.c_int)
@@ -89,13 +92,15 @@ class Port:
 
     @classmethod
     def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3,
-               eig="full"):
+               eig="full", dnx=None, dny=None, dnz=None):
+        """dnx/dny/dnz: the problem's tables (NULL: periodic)."""
         nz, ny, nx = s["ro"].shape
+        tab = lambda t: None if t is None else (C.c_int * 8)(*[int(x) for x in t])
         with cls._eig(eig):
-            cls.lib().oracle_fd_ct_3d(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by",
-                                                       "bz")],
-                                      dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma, odr,
-                                      _flux_id(flux), nrk)
+            cls.lib().oracle_fd_ct_3d_bc(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by",
+                                                          "bz")],
+                                         dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma, odr,
+                                         _flux_id(flux), nrk, tab(dnx), tab(dny), tab(dnz))
 
     @classmethod
     def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3, dnx=None,
@@ -228,11 +233,22 @@ class Ref:
 
     @classmethod
     def step3d(cls, s, dt, dx, dy, dz, off=4, gamma=5 / 3, odr=4, flux="mlau", nrk=3,
-               eig="full"):
+               eig="full", dnx=None, dny=None, dnz=None):
+        """dnx/dny/dnz: tables written into the build's dnxs/dnys/dnzs for this
+        call; None is periodic."""
         nz, ny, nx = s["ro"].shape
-        cls._get(3, odr, _flux_id(flux), nrk, eig=eig).ref_step(
-            *[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
-            dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma)
+        lib = cls._get(3, odr, _flux_id(flux), nrk, eig=eig)
+        gs = [(C.c_int * 8).in_dll(lib, nm) for nm in ("dnxs", "dnys", "dnzs")]
+        for g, t in zip(gs, (dnx, dny, dnz)):
+            for v in range(8):
+                g[v] = 0 if t is None else int(t[v])
+        try:
+            lib.ref_step(*[s[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                         dt, dx, dy, dz, nx, ny, nz, off, off, off, gamma)
+        finally:
+            for g in gs:
+                for v in range(8):
+                    g[v] = 0
 
     @classmethod
     def step2d(cls, s, dt, dx, dy, off=4, gamma=5 / 3, odr=4, flux="lhlld", nrk=3, dnx=None,

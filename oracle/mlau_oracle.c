@@ -19,6 +19,8 @@
    drivers' choice) or 2 (Miyoshi's mhd_m_reconst swapped in). */
 static int o_full = 1;
 
+static const int o_zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
 void oracle_set_eigen(int miyoshi) { o_full = miyoshi ? 2 : 1; }
 
 /* Phase hook of the op-counting build (oracle/opcount.cpp); no-op here.
@@ -47,32 +49,63 @@ static void rk_coef(int nrk, int stage, double *a, double *b)
     *b = t[stage][1];
 }
 
-/* Periodic ghost fill of one 3D array: X, then Y, then Z, each over the full
- * extent of the other axes (single-rank branch of mpi_sdrv3d,
- * 3D/MPI/OTvortex/boundary.c:91-104,150-163,209-222). */
-static void fill3d(double *f, int nx, int ny, int nz, int xoff, int yoff, int zoff)
+/* Ghost fill of one 3D array as the MPI driver leaves it for one rank
+ * (3D/MPI/OTvortex/boundary.c): the periodic exchange along each axis whose
+ * table entry 0 (dn0) is zero (mpi_sdrv3d), then the X, Y and Z mirrors by
+ * dn (mpi_xbc3d / _ybc3d / _zbc3d, :227-309): dn -1 Dirichlet, +1 Neumann,
+ * 0 nothing; st 1 marks a face-centred axis (its right boundary face is
+ * kept). */
+static void fill3d_bc(double *f, int nx, int ny, int nz, int xoff, int yoff, int zoff,
+                      const int dn0[3], const int st[3], const int dn[3])
 {
-#pragma omp parallel for
-    for (int k = 0; k < nz; k++)
-        for (int j = 0; j < ny; j++)
-            for (int i = 0; i < xoff; i++) {
-                f[IDX3(nx - 1 - i, j, k)] = f[IDX3(2 * xoff - 1 - i, j, k)];
-                f[IDX3(i, j, k)] = f[IDX3(nx - 2 * xoff + i, j, k)];
+    if (dn0[0] == 0)
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < xoff; i++) {
+                    f[IDX3(nx - 1 - i, j, k)] = f[IDX3(2 * xoff - 1 - i, j, k)];
+                    f[IDX3(i, j, k)] = f[IDX3(nx - 2 * xoff + i, j, k)];
+                }
+    if (dn0[1] == 0)
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < yoff; j++)
+                for (int i = 0; i < nx; i++) {
+                    f[IDX3(i, ny - 1 - j, k)] = f[IDX3(i, 2 * yoff - 1 - j, k)];
+                    f[IDX3(i, j, k)] = f[IDX3(i, ny - 2 * yoff + j, k)];
+                }
+    if (dn0[2] == 0)
+        for (int k = 0; k < zoff; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) {
+                    f[IDX3(i, j, nz - 1 - k)] = f[IDX3(i, j, 2 * zoff - 1 - k)];
+                    f[IDX3(i, j, k)] = f[IDX3(i, j, nz - 2 * zoff + k)];
+                }
+    if (dn[0] != 0)
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++) {
+                for (int i = 0; i < xoff; i++)
+                    f[IDX3(i, j, k)] = dn[0] * f[IDX3((2 * xoff - 1 + st[0]) - i, j, k)];
+                for (int i = 0; i < xoff - st[0]; i++)
+                    f[IDX3(nx - 1 - i, j, k)] = dn[0] * f[IDX3((nx - 2 * xoff + st[0]) + i, j, k)];
             }
-#pragma omp parallel for
-    for (int k = 0; k < nz; k++)
-        for (int j = 0; j < yoff; j++)
-            for (int i = 0; i < nx; i++) {
-                f[IDX3(i, ny - 1 - j, k)] = f[IDX3(i, 2 * yoff - 1 - j, k)];
-                f[IDX3(i, j, k)] = f[IDX3(i, ny - 2 * yoff + j, k)];
-            }
-#pragma omp parallel for
-    for (int k = 0; k < zoff; k++)
-        for (int j = 0; j < ny; j++)
-            for (int i = 0; i < nx; i++) {
-                f[IDX3(i, j, nz - 1 - k)] = f[IDX3(i, j, 2 * zoff - 1 - k)];
-                f[IDX3(i, j, k)] = f[IDX3(i, j, nz - 2 * zoff + k)];
-            }
+    if (dn[1] != 0)
+        for (int k = 0; k < nz; k++) {
+            for (int j = 0; j < yoff; j++)
+                for (int i = 0; i < nx; i++)
+                    f[IDX3(i, j, k)] = dn[1] * f[IDX3(i, (2 * yoff - 1 + st[1]) - j, k)];
+            for (int j = 0; j < yoff - st[1]; j++)
+                for (int i = 0; i < nx; i++)
+                    f[IDX3(i, ny - 1 - j, k)] = dn[1] * f[IDX3(i, (ny - 2 * yoff + st[1]) + j, k)];
+        }
+    if (dn[2] != 0) {
+        for (int k = 0; k < zoff; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++)
+                    f[IDX3(i, j, k)] = dn[2] * f[IDX3(i, j, (2 * zoff - 1 + st[2]) - k)];
+        for (int k = 0; k < zoff - st[2]; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++)
+                    f[IDX3(i, j, nz - 1 - k)] = dn[2] * f[IDX3(i, j, (nz - 2 * zoff + st[2]) + k)];
+    }
 }
 
 /* bc2d, 2D/SERIAL/OTvortex/boundary.c:18-74: one array, X then Y; dn 0 is
@@ -232,13 +265,18 @@ static void emf_pencil(const double *fu, const double *fc, const double *ctw, in
 }
 
 /* ------------------------------------------------------------------------ */
-/* 3D driver: 3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-1198, one rank, periodic.     */
+/* 3D driver: 3D/MPI/OTvortex/mhd_fd_ct_3d.c:99-1198, one rank, with the    */
+/* problem's tables dnxs/dnys/dnzs (NULL: periodic).                          */
 /* ------------------------------------------------------------------------ */
-void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
-                     double *by, double *bz, double dt, double dx, double dy, double dz,
-                     int nx, int ny, int nz, int xoff, int yoff, int zoff, double gamma,
-                     int odr, int flx, int nrk)
+void oracle_fd_ct_3d_bc(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                        double *by, double *bz, double dt, double dx, double dy, double dz,
+                        int nx, int ny, int nz, int xoff, int yoff, int zoff, double gamma,
+                        int odr, int flx, int nrk, const int *tx_in, const int *ty_in,
+                        const int *tz_in)
 {
+    const int *tx = tx_in ? tx_in : o_zero8, *ty = ty_in ? ty_in : o_zero8,
+              *tz = tz_in ? tz_in : o_zero8;
+    const int dn0[3] = {tx[0], ty[0], tz[0]}, st0[3] = {0, 0, 0};
     const long n = (long)nx * ny * nz;
     const double dtdx = dt / dx, dtdy = dt / dy, dtdz = dt / dz;
     double *state[8] = {ro, mx, my, mz, bx, by, bz, en};
@@ -284,9 +322,13 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
                     long s = IDX3(i, j, k);
                     cz[s] = o_face2cen(odr, bz[s - sz], bz[s], bz[s + sz], bz[s + 2 * sz]);
                 }
-        fill3d(cx, nx, ny, nz, xoff, yoff, zoff);
-        fill3d(cy, nx, ny, nz, xoff, yoff, zoff);
-        fill3d(cz, nx, ny, nz, xoff, yoff, zoff);
+        {
+            const int d5[3] = {tx[5], ty[5], tz[5]}, d6[3] = {tx[6], ty[6], tz[6]},
+                      d7[3] = {tx[7], ty[7], tz[7]};
+            fill3d_bc(cx, nx, ny, nz, xoff, yoff, zoff, dn0, st0, d5);
+            fill3d_bc(cy, nx, ny, nz, xoff, yoff, zoff, dn0, st0, d6);
+            fill3d_bc(cz, nx, ny, nz, xoff, yoff, zoff, dn0, st0, d7);
+        }
 
         /* primitives (:240-262) */
 #pragma omp parallel for
@@ -361,9 +403,14 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
                     dvy[s] = o_min((vy[s + sy] - vy[s]), (vy[s] - vy[s - sy]));
                     dvz[s] = o_min((vz[s + sz] - vz[s]), (vz[s] - vz[s - sz]));
                 }
-        fill3d(dvx, nx, ny, nz, xoff, yoff, zoff);
-        fill3d(dvy, nx, ny, nz, xoff, yoff, zoff);
-        fill3d(dvz, nx, ny, nz, xoff, yoff, zoff);
+        {
+            /* the sensors' sign flips (:367-376) */
+            const int d1[3] = {-tx[1], +ty[1], +tz[1]}, d2[3] = {+tx[2], -ty[2], +tz[2]},
+                      d3[3] = {+tx[3], +ty[3], -tz[3]};
+            fill3d_bc(dvx, nx, ny, nz, xoff, yoff, zoff, dn0, st0, d1);
+            fill3d_bc(dvy, nx, ny, nz, xoff, yoff, zoff, dn0, st0, d2);
+            fill3d_bc(dvz, nx, ny, nz, xoff, yoff, zoff, dn0, st0, d3);
+        }
 
         /* three face sweeps; rotated variables (:379-493, :587-701, :795-909) */
         sweep_in SX = {ro, vx, vy, vz, cx, cy, cz, pr, m2, bx, dvy, dvz, 1, 1};
@@ -473,8 +520,13 @@ void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en,
                     double d1 = o_diff(odr, ex[s - sy], ex[s], ex[s + sy], ex[s + 2 * sy]);
                     bz[s] = ra * u0[6 * n + s] + rb * (bz[s] - dtdx * d0 + dtdy * d1);
                 }
-        /* periodic boundary of the 8 conserved arrays (:1161-1175) */
-        for (int v = 0; v < 8; v++) fill3d(state[v], nx, ny, nz, xoff, yoff, zoff);
+        /* boundary of the 8 conserved arrays (:1161-1175); state[] holds
+           ro mx my mz bx by bz en, the tables ro mx my mz en bx by bz */
+        for (int v = 0; v < 8; v++) {
+            const int t = (v < 4) ? v : (v == 7 ? 4 : v + 1);
+            const int st[3] = {t == 5, t == 6, t == 7}, dn[3] = {tx[t], ty[t], tz[t]};
+            fill3d_bc(state[v], nx, ny, nz, xoff, yoff, zoff, dn0, st, dn);
+        }
     }
 
     free(u0);
@@ -962,7 +1014,6 @@ static void o_bc2d_mpi(double **p, int nn, const int *stx, const int *sty, const
     }
 }
 
-static const int o_zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
 /* diff_ctfield_e (2D/MPI/MRX/mhd_fd_ct_2d.c:726-950): resistive diffusion of
    the CT field with uniform resistivity eta0, energy updated by the
@@ -1377,5 +1428,14 @@ void oracle_inj_ro(double *ro, double *mx, double *my, double *mz, double *en, d
     }
     double *p[8] = {ro, mx, my, mz, en, bx, by, bz};
     o_sdrv2d(p, 8, dnx[0], dny[0], nx, ny, xoff, yoff);
+}
+
+void oracle_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                     double *by, double *bz, double dt, double dx, double dy, double dz,
+                     int nx, int ny, int nz, int xoff, int yoff, int zoff, double gamma,
+                     int odr, int flx, int nrk)
+{
+    oracle_fd_ct_3d_bc(ro, mx, my, mz, en, bx, by, bz, dt, dx, dy, dz, nx, ny, nz, xoff, yoff,
+                       zoff, gamma, odr, flx, nrk, NULL, NULL, NULL);
 }
 

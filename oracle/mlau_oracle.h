@@ -116,6 +116,13 @@ void oracle_inj_ro(double *ro, double *mx, double *my, double *mz, double *en, d
                    double dro3, double vy_1, double bx_1, double by_1, double bz_1, double pr_1,
                    double vref, double gam, const double *noise, const int *dnx,
                    const int *dny);
+/* The 3D step with the problem's tables dnxs/dnys/dnzs (NULL: periodic),
+ * filled as the MPI driver's single-rank routines do. */
+void oracle_fd_ct_3d_bc(double *ro, double *mx, double *my, double *mz, double *en, double *bx,
+                        double *by, double *bz, double dt, double dx, double dy, double dz,
+                        int nx, int ny, int nz, int xoff, int yoff, int zoff, double gamma,
+                        int odr, int flx, int nrk, const int *dnx, const int *dny,
+                        const int *dnz);
 /* Eigen-system of the oracle's steps where Mach^2 >= 1: 0 the drivers' full
  * 7-wave system, 1 Miyoshi's (the driver with mhd_c_reconst swapped for
  * mhd_m_reconst). */

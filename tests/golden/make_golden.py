@@ -85,6 +85,13 @@ CASES_MRX = [
     ("mrx2d_o4_rk3_cond_walls", 20, 24, 4, 4, 3, 26, WALLS, MRX_TABLES[1], 2.0),
 ]
 MRX_LOOPS = (1, 3)
+# 3D with boundary tables (the MPI driver's mirrors), whole arrays stored:
+# (name, n, odr, flux, seed, dnx, dny, dnz)
+CASES_3D_WALLS = [
+    ("3d_mlau_o4_walls", 6, 4, "mlau", 31, (0,) * 8, (1, 1, -1, 1, 1, 1, -1, 1),
+     (1, 1, 1, -1, 1, 1, 1, -1)),
+    ("3d_lhlld_o2_walls", 6, 2, "lhlld", 32, (1, -1, 1, 1, 1, -1, 1, 1), (1,) * 8, (0,) * 8),
+]
 # The RMI problem's main loop (2D/MPI/RMI/main.cpp:46-58): the inflow at the
 # upper boundary (inj_ro, with its random() density perturbation drawn after
 # srandom(seed + loop)), the periodic exchange along x, the MPI 2D step (ODR 2,
@@ -216,6 +223,26 @@ def main(only=()):
             done = nloop
             for k, v in s.items():
                 out[f"out{nloop}_" + k] = v.copy()
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    for name, n, odr, flux, seed, dnx, dny, dnz in CASES_3D_WALLS:
+        if skip(name):
+            continue
+        st, m = ics.turbulence_3d(n=n, ny=n + 1, nz=n - 1, mach=0.8, seed=seed, odr=odr)
+        dt = 0.3 * m["dx"] / m["vfast"]
+        out = {"dim": 3, "dt": dt, "dx": m["dx"], "dy": m["dy"], "dz": m["dz"], "gamma": m["gamma"],
+               "odr": odr, "flux": flux, "dnx": np.array(dnx), "dny": np.array(dny),
+               "dnz": np.array(dnz)}
+        for k, v in st.items():
+            out["in_" + k] = v.copy()
+        s = ics.copy_state(st)
+        done = 0
+        for nstep in STEPS:
+            for _ in range(nstep - done):
+                Ref.step3d(s, dt, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux, dnx=dnx, dny=dny,
+                           dnz=dnz)
+            done = nstep
+            for k, v in s.items():
+                out[f"out{nstep}_" + k] = v.copy()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     for name, n, ny, seed in CASES_RMI:
         if skip(name):

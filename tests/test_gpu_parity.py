@@ -24,11 +24,13 @@ def gpu_run(dim, st, steps, dt, **kw):
     eig = kw.pop("eig", "full")
     with M.Sim(dim, st["ro"].shape, **kw) as s:
         s.set_eigen(eig)
+        if tables is not None and dim == 3:
+            s.set_bc3d(*tables)
         if bx is not None:
             s.set_bx(bx)
         if bc is not None:
             s.set_bc(bc)
-        if tables is not None:
+        if tables is not None and dim == 2:
             s.set_bc2d(*tables)
         s.upload(st)
         s.step(dt, steps)
@@ -40,9 +42,10 @@ def gpu_run(dim, st, steps, dt, **kw):
 def test_golden_3d(name):
     prm, s, outs = load_golden(name)
     for n, ref in outs.items():
-        got = gpu_run(3, s, n, prm["dt"], dx=prm["dx"], dy=prm["dx"], dz=prm["dx"],
-                      gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"],
-                      eig=prm.get("eig", "full"))
+        tables = (prm["dnx"], prm["dny"], prm["dnz"]) if "dnx" in prm else None
+        got = gpu_run(3, s, n, prm["dt"], dx=prm["dx"], dy=prm.get("dy", prm["dx"]),
+                      dz=prm.get("dz", prm["dx"]), gamma=prm["gamma"], odr=prm["odr"],
+                      flux=prm["flux"], eig=prm.get("eig", "full"), tables=tables)
         assert equal_values(got, ref), f"{name} after {n} steps: {max_rel_diff(got, ref)}"
 
 

@@ -102,3 +102,91 @@ def test_dropin_driver_applies_the_problem_tables(port, tmp_path):
     for _ in range(3):
         port.step2d(ref, dt, m["dx"], m["dy"], odr=2, flux="lhlld", dnx=KHI[0], dny=KHI[1])
     assert equal_values(got, ref), max_rel_diff(got, ref)
+
+
+# --- 3D: the MPI driver's tables ------------------------------------------------
+Z8, W8, N8 = (0,) * 8, (1, -1, 1, 1, 1, -1, 1, 1), (1,) * 8
+WY8, WZ8 = (1, 1, -1, 1, 1, 1, -1, 1), (1, 1, 1, -1, 1, 1, 1, -1)
+TABLES_3D = [(Z8, Z8, WZ8), (W8, Z8, Z8), (Z8, WY8, Z8), (W8, WY8, WZ8), (N8, N8, N8)]
+
+
+@pytest.mark.parametrize("tables", TABLES_3D)
+@pytest.mark.parametrize("odr,flux", list(itertools.product((1, 2, 3, 4, 5, 6),
+                                                             ("mlau", "lhlld", "hlld", "roe"))))
+def test_walls_3d_vs_oracle(port, odr, flux, tables):
+    """The 3D step with Dirichlet / Neumann mirrors on any axes (cell B, the
+    shock sensors with their sign flips, the conserved arrays, the right
+    boundary faces) against the oracle, which equals the reference driver
+    built with the tables."""
+    st, m = ics.turbulence_3d(n=8, ny=9, nz=7, mach=0.6, seed=odr * 3 + len(flux), odr=odr)
+    dt = 0.3 * m["dx"] / m["vfast"]
+    ref = ics.copy_state(st)
+    for _ in range(3):
+        port.step3d(ref, dt, m["dx"], m["dy"], m["dz"], odr=odr, flux=flux, dnx=tables[0],
+                    dny=tables[1], dnz=tables[2])
+    with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"], odr=odr, flux=flux) as s:
+        s.set_bc3d(*tables)
+        s.upload(st)
+        s.step(dt, 3)
+        got = s.download()
+    assert equal_values(got, ref, equal_nan=True), max_rel_diff(got, ref)
+
+
+def test_walls_3d_many_steps_keep_div_b(port):
+    """40 steps with walls on all three axes (graph replay included): equal
+    values to the oracle and the interior div B kept at round-off."""
+    tables = TABLES_3D[3]
+    st, m = ics.turbulence_3d(n=16, ny=12, nz=10, mach=0.3, seed=5)
+    dt = 0.3 * m["dx"] / m["vfast"]
+    ref = ics.copy_state(st)
+    for _ in range(40):
+        port.step3d(ref, dt, m["dx"], m["dy"], m["dz"], dnx=tables[0], dny=tables[1],
+                    dnz=tables[2])
+    with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"]) as s:
+        s.set_bc3d(*tables)
+        s.upload(st)
+        s.step(dt, 1)
+        first = s.download()
+        s.step(dt, 39)
+        got = s.download()
+    assert equal_values(got, ref)
+    # the periodic initial ghosts move the boundary faces in the first step;
+    # from then on the CT update keeps div B
+    assert ics.div_b_3d(got, m["dx"], m["dy"], m["dz"], base=first) <= 1e-12
+
+
+def test_dropin_3d_tables(port):
+    """mhd_fd_ct_3d through the reference signature with the library's
+    dnxs/dnys/dnzs set as a problem program would; mixed tables on one axis
+    are refused with the arrays unchanged."""
+    import ctypes as C
+
+    L = M.lib()
+    gs = [(C.c_int * 8).in_dll(L, nm) for nm in ("dnxs", "dnys", "dnzs")]
+    tables = TABLES_3D[3]
+    st, m = ics.turbulence_3d(n=8, mach=0.5, seed=21)
+    dt = 0.3 * m["dx"] / m["vfast"]
+    nz, ny, nx = st["ro"].shape
+    M.set_scheme(3, 4, "mlau", 3)
+    try:
+        for g, t in zip(gs, tables):
+            for v in range(8):
+                g[v] = t[v]
+        ref, got = ics.copy_state(st), ics.copy_state(st)
+        port.step3d(ref, dt, m["dx"], m["dy"], m["dz"], dnx=tables[0], dny=tables[1],
+                    dnz=tables[2])
+        M.mhd_fd_ct_3d(*[got[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")], dt,
+                       m["dx"], m["dy"], m["dz"], nx, ny, nz, 4, 4, 4, m["gamma"])
+        assert equal_values(got, ref)
+        gs[1][0] = 0
+        before = ics.copy_state(got)
+        with pytest.raises(M.MlauError, match="all zero or all nonzero"):
+            M.mhd_fd_ct_3d(*[got[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                           dt, m["dx"], m["dy"], m["dz"], nx, ny, nz, 4, 4, 4, m["gamma"])
+        assert equal_values(got, before)
+    finally:
+        for g in gs:
+            for v in range(8):
+                g[v] = 0
+        M.set_scheme(3, 2, "lhlld", 3)
+        M.release_dropin()

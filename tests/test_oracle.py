@@ -16,8 +16,10 @@ def test_port_matches_golden_3d(port, name):
     done = 0
     for n in sorted(outs):
         for _ in range(n - done):
-            port.step3d(s, prm["dt"], prm["dx"], prm["dx"], prm["dx"], gamma=prm["gamma"],
-                        odr=prm["odr"], flux=prm["flux"], eig=prm.get("eig", "full"))
+            port.step3d(s, prm["dt"], prm["dx"], prm.get("dy", prm["dx"]), prm.get("dz", prm["dx"]),
+                        gamma=prm["gamma"], odr=prm["odr"], flux=prm["flux"],
+                        eig=prm.get("eig", "full"), dnx=prm.get("dnx"), dny=prm.get("dny"),
+                        dnz=prm.get("dnz"))
         done = n
         assert equal_values(s, outs[n]), f"{name}: differs after {n} steps"
 
@@ -316,4 +318,26 @@ def test_inflow_matches_reference(port, seed, perturb):
             f[:, i] = f[:, nx - 8 + i]
     assert equal_values(a, b)
     assert not equal_values(a, st)
+
+
+Z8, W8, N8 = (0,) * 8, (1, -1, 1, 1, 1, -1, 1, 1), (1,) * 8
+TABLES_3D = [(Z8, Z8, (1, 1, 1, -1, 1, 1, 1, -1)), (W8, Z8, Z8), (Z8, (1, 1, -1, 1, 1, 1, -1, 1), Z8),
+             (W8, (1, 1, -1, 1, 1, 1, -1, 1), (1, 1, 1, -1, 1, 1, 1, -1)), (N8, N8, N8)]
+
+
+@needs_ref
+@pytest.mark.parametrize("tables", TABLES_3D)
+@pytest.mark.parametrize("odr,flux", [(4, "mlau"), (2, "lhlld"), (3, "hlld"), (5, "mlau"),
+                                      (1, "roe")])
+def test_port_matches_reference_3d_tables(port, odr, flux, tables):
+    """The 3D step with the problem's tables (the MPI driver's exchange and
+    mirrors at its three fill sites) against the reference driver built with
+    the same tables."""
+    st, m = ics.turbulence_3d(n=6, ny=7, nz=5, mach=0.8, seed=odr + len(flux), odr=odr)
+    a, b = ics.copy_state(st), ics.copy_state(st)
+    kw = dict(odr=odr, flux=flux, dnx=tables[0], dny=tables[1], dnz=tables[2])
+    for _ in range(2):
+        port.step3d(a, 1e-3, m["dx"], m["dy"], m["dz"], **kw)
+        Ref.step3d(b, 1e-3, m["dx"], m["dy"], m["dz"], **kw)
+    assert equal_values(a, b, equal_nan=True)
 
