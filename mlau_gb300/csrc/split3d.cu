@@ -1,12 +1,18 @@
 // FP32-split 3D step.  Same scheme and data layout as the plain FP64 step
 // (3D/MPI/OTvortex/mhd_fd_ct_3d.c), with the arithmetic split by what needs
-// FP64:
+// more than FP32:
 //
-//   FP64  conserved state, its RK3 accumulation of flux differences, primitive
-//         recovery p = (gamma-1)(E - rho v^2/2 - B^2/2) (cancellation at low
-//         Mach and low beta), the CT curl update of face B (div B at round-off).
+//   float-float (~48 bits, FP32 pipe; the state is stored in FP64)
+//         the RK3 accumulation of flux differences into the conserved state,
+//         primitive recovery p = (gamma-1)(E - rho v^2/2 - B^2/2) and cell B
+//         (cancellation at low Mach and low beta), the CT curl update of face
+//         B (div B at round-off).
 //   FP32  characteristic reconstruction and the Riemann solver, the edge EMFs,
 //         the CT weights and shock sensors.
+//
+// On this part FP64 issues at 1/64 of the FP32 rate, so the 48-bit parts run
+// as float-float arithmetic (ff.cuh) rather than FP64: 10-20 FP32 operations
+// per FP64 one still leave the prep and update kernels near the memory roof.
 //
 // Reconstruction works on perturbations from the cell centre, q_m - q_c, and
 // WCNS/MUSCL/linear weights are translation invariant, so the face states
@@ -14,16 +20,16 @@
 // The Riemann solver receives its total-pressure and normal-velocity jumps
 // formed the same way (centre difference + perturbation difference).
 //
-// The primitives leave the FP64 prep kernel as (hi, lo) float pairs with
+// The primitives leave the prep kernel as (hi, lo) float pairs with
 // q = hi + lo to ~48 bits, so every later difference q_m - q_c is formed in
 // FP32 as (hi_m - hi_c) + (lo_m - lo_c) without losing the perturbation.
 // Flux differences are formed in FP32 (neighbouring fluxes of one sign
-// subtract exactly) and added to the FP64 state in FP64.
+// subtract exactly) and added to the state in float-float.
 //
-// Kernels per RK stage: prep (FP64 primitive recovery -> float pairs), aux
-// (FP32 CT weights and shock sensors), one fused reconstruction + flux kernel
-// per direction, emf (FP32), update (FP64 RK combine + CT curl + periodic
-// ghost images).
+// Kernels per RK stage: prep (float-float primitive recovery -> float pairs),
+// aux (FP32 CT weights and shock sensors), one fused reconstruction + flux
+// kernel per direction, emf (FP32), update (float-float RK combine + CT curl +
+// periodic ghost images).
 //
 // The fused sweep is a persistent kernel over tiles.  Each tile's inputs (the
 // 5-point stencils of eight float-pair arrays and four float arrays, halo
@@ -40,6 +46,7 @@
 #include "point.cuh"
 #include "tma.cuh"
 #include "split_conv.cuh"
+#include "ff.cuh"
 
 #include <algorithm>
 
@@ -95,43 +102,72 @@ struct Dims {
     }
 };
 
-// --- primitives (FP64 recovery, FP32-pair output) ------------------------
-__global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, double gamma, float gamma_f)
+// Cell of this thread for the whole-grid kernels: one thread per cell of an
+// x-y plane (flattened, so no block runs mostly past the row end), one grid
+// row of blocks per z-plane.
+__device__ __forceinline__ bool plane_cell(const Dims &d, int &i, int &j, int &k)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-    if (i >= d.nx) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.nx * d.ny) return false;
+    j = t / d.nx;
+    i = t - j * d.nx;
+    k = blockIdx.y;
+    return true;
+}
+
+// A host double as a float-float pair (hi rounded, lo the rounded rest).
+inline float2 host_ff(double x)
+{
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+
+// --- primitives (float-float recovery, FP32-pair output) -----------------
+// Face-to-centre B as the scheme's calc_bc, in float-float.
+__device__ __forceinline__ ff face2cen_ff(int odr, const double *b, long long w, long long st)
+{
+    const ff f1 = ff_from(b[w]), f2 = ff_from(b[w + st]);
+    if (lin_odr(odr) <= 2) return ff_scale(ff_add(f1, f2), 0.5f);
+    const ff f0 = ff_from(b[w - st]), f3 = ff_from(b[w + 2 * st]);
+    return ff_scale(ff_sub(ff_mul_f(ff_add(f1, f2), 9.0f), ff_add(f0, f3)), 0.0625f);
+}
+
+__global__ void __launch_bounds__(256)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f)
+{
+    int i, j, k;
+    if (!plane_cell(d, i, j, k)) return;
     const long long sy = d.nx, sz = (long long)d.nx * d.ny;
     const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
-    const double *bx = f.s[5], *by = f.s[6], *bz = f.s[7];
-    const double cx = face2cen(odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
-    const double cy = face2cen(odr, by[w - sy], by[w], by[w + sy], by[w + 2 * sy]);
-    const double cz = face2cen(odr, bz[w - sz], bz[w], bz[w + sz], bz[w + 2 * sz]);
+    const ff cx = face2cen_ff(odr, f.s[5], w, 1);
+    const ff cy = face2cen_ff(odr, f.s[6], w, sy);
+    const ff cz = face2cen_ff(odr, f.s[7], w, sz);
     const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
     const double ro = f.s[0][s];
     // Velocities and the kinetic energy in FP32: rho v^2/2 enters the pressure
     // as an additive term, so its FP32 rounding (1e-7 of itself) stays below
     // the pressure's own FP32 resolution at any Mach number; the cancelling
-    // terms E and B^2/2 stay FP64.
+    // terms E and B^2/2 are carried in float-float (48 bits).
     const float2 ro2 = split2(ro);
     const float rof = ro2.x + ro2.y, irof = 1.0f / rof;
     const float vx = to_f32(f.s[1][s]) * irof, vy = to_f32(f.s[2][s]) * irof,
                 vz = to_f32(f.s[3][s]) * irof;
     const float v2 = vx * vx + vy * vy + vz * vz;
-    const double b2 = cx * cx + cy * cy + cz * cz;
-    const double pr = (gamma - 1) * (f.s[4][s] - 0.5 * (to_f64(rof * v2) + b2));
-    const float2 pr2 = split2(pr);
+    const ff b2 = ff_add(ff_add(ff_sqr(cx), ff_sqr(cy)), ff_sqr(cz));
+    const ff pr = ff_mul({gm1.x, gm1.y},
+                         ff_sub(ff_from(f.s[4][s]), ff_scale(ff_add_f(b2, rof * v2), 0.5f)));
+    const float2 pr2 = ff_pair(pr);
     g.q[0][sp] = ro2;
     g.q[1][sp] = make_float2(vx, 0.f);
     g.q[2][sp] = make_float2(vy, 0.f);
     g.q[3][sp] = make_float2(vz, 0.f);
-    g.q[4][sp] = split2(cx);
-    g.q[5][sp] = split2(cy);
-    g.q[6][sp] = split2(cz);
+    g.q[4][sp] = ff_pair(cx);
+    g.q[5][sp] = ff_pair(cy);
+    g.q[6][sp] = ff_pair(cz);
     g.q[7][sp] = pr2;
-    g.bf[0][sp] = to_f32(bx[s]);
-    g.bf[1][sp] = to_f32(by[s]);
-    g.bf[2][sp] = to_f32(bz[s]);
+    g.bf[0][sp] = to_f32(f.s[5][s]);
+    g.bf[1][sp] = to_f32(f.s[6][s]);
+    g.bf[2][sp] = to_f32(f.s[7][s]);
     g.m2[sp] = v2 / (gamma_f * (pr2.x + pr2.y) * irof);
 }
 
@@ -162,8 +198,8 @@ __device__ __forceinline__ float ct_w(const float2 *va, const float2 *vb, const 
 
 __global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-    if (i >= d.nx) return;
+    int i, j, k;
+    if (!plane_cell(d, i, j, k)) return;
     const long long sy = d.px, sz = d.px * d.ny;
     const long long s = d.ap(i, j, k);
     const float2 *ro = g.q[0], *vx = g.q[1], *vy = g.q[2], *vz = g.q[3];
@@ -417,8 +453,8 @@ __device__ __forceinline__ float emf_part32(const float *fu, const float *fc, fl
 
 __global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-    if (i >= d.nx) return;
+    int i, j, k;
+    if (!plane_cell(d, i, j, k)) return;
     const long long sy = d.px, sz = d.px * d.ny;
     const long long c = d.ap(i, j, k);
     const bool xi = (i >= 3 && i < d.nx - 2), yj = (j >= 3 && j < d.ny - 2),
@@ -453,19 +489,33 @@ __device__ __forceinline__ float df32(int odr, const float *f, long long s, long
     return fdiff(odr, f[s - st], f[s], f[s + st], f[s + 2 * st]);
 }
 
-// FP64 difference of the (FP32-valued) edge EMFs along one axis, without the
-// 1/24 of the 4th-order stencil (folded into dt/dx by the caller): every
-// operation is exact, so the discrete divergence of the curl cancels.
-__device__ __forceinline__ double df64(int odr, const double *f, long long s, long long st)
+// Float-float difference of the (FP32-valued) edge EMFs along one axis,
+// without the 1/24 of the 4th-order stencil (folded into dt/dx by the
+// caller): the differences of two floats are exact as float-float, and so is
+// 27 times one, so the discrete divergence of the curl cancels to the
+// float-float round-off.
+__device__ __forceinline__ ff df_ff(int odr, const double *f, long long s, long long st)
 {
-    const double f0 = f[s - st], f1 = f[s], f2 = f[s + st], f3 = f[s + 2 * st];
-    if (lin_odr(odr) <= 2) return f2 - f1;
-    return 27.0 * (f2 - f1) - (f3 - f0);
+    const float f1 = to_f32(f[s]), f2 = to_f32(f[s + st]);
+    if (lin_odr(odr) <= 2) return ff_two_sum(f2, -f1);
+    const float f0 = to_f32(f[s - st]), f3 = to_f32(f[s + 2 * st]);
+    return ff_sub(ff_mul_f(ff_two_sum(f2, -f1), 27.0f), ff_two_sum(f3, -f0));
+}
+
+// The RK combine ra u0 + rb u in float-float (ra = 0, rb = 1 at the first stage).
+struct RkFF {
+    float2 ra, rb;
+    int first;
+};
+__device__ __forceinline__ double rk_ff(const RkFF &c, const double *u0, long long s, ff u)
+{
+    if (c.first) return ff_to_double(u);
+    return ff_to_double(ff_add(ff_mul({c.ra.x, c.ra.y}, ff_from(u0[s])), ff_mul({c.rb.x, c.rb.y}, u)));
 }
 
 __global__ void __launch_bounds__(256)
-ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, double ra, double rb, float dtdx,
-          float dtdy, float dtdz, double dtdx_d, double dtdy_d, double dtdz_d)
+ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, float dtdx, float dtdy,
+          float dtdz, float2 ddx2, float2 ddy2, float2 ddz2)
 {
     const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = d.oy + blockIdx.y, k = d.oz + blockIdx.z;
@@ -478,19 +528,21 @@ ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, double ra, double rb, flo
     for (int v = 0; v < 5; v++) {
         const float div = dtdx * df32(odr, g.F[0][cX[v]], sp, 1) + dtdy * df32(odr, g.F[1][cY[v]], sp, sy)
                           + dtdz * df32(odr, g.F[2][cZ[v]], sp, sz);
-        out[v] = ra * f.u0[v][s] + rb * (f.s[v][s] - to_f64(div));
+        // the first stage is u - div: one FP64 addition beats its float-float form
+        out[v] = rk.first ? f.s[v][s] - to_f64(div)
+                          : rk_ff(rk, f.u0[v], s, ff_add_f(ff_from(f.s[v][s]), -div));
     }
-    // CT curl in FP64: the differences of the FP32 edge EMFs are exact in
-    // FP64, so the discrete divergence of the B increment cancels to FP64
-    // round-off (in FP32, 27*(E2-E1) alone would need more than 24 bits).
-    // dtdx_d etc. carry the stencil's 1/24 when odr > 2.
-    const double ddx = dtdx_d, ddy = dtdy_d, ddz = dtdz_d;
-    out[5] = ra * f.u0[5][s] + rb * (f.s[5][s] - ddy * df64(odr, g.e[2], sp, sy)
-                                     + ddz * df64(odr, g.e[1], sp, sz));
-    out[6] = ra * f.u0[6][s] + rb * (f.s[6][s] - ddz * df64(odr, g.e[0], sp, sz)
-                                     + ddx * df64(odr, g.e[2], sp, 1));
-    out[7] = ra * f.u0[7][s] + rb * (f.s[7][s] - ddx * df64(odr, g.e[1], sp, 1)
-                                     + ddy * df64(odr, g.e[0], sp, sy));
+    // CT curl in float-float: the differences of the FP32 edge EMFs are
+    // exact, so the discrete divergence of the B increment cancels to the
+    // float-float round-off (in FP32, 27*(E2-E1) alone would need more than
+    // 24 bits).  ddx2 etc. carry the stencil's 1/24 when odr > 2.
+    const ff ddx = {ddx2.x, ddx2.y}, ddy = {ddy2.x, ddy2.y}, ddz = {ddz2.x, ddz2.y};
+    out[5] = rk_ff(rk, f.u0[5], s, ff_add(ff_sub(ff_from(f.s[5][s]), ff_mul(ddy, df_ff(odr, g.e[2], sp, sy))),
+                                          ff_mul(ddz, df_ff(odr, g.e[1], sp, sz))));
+    out[6] = rk_ff(rk, f.u0[6], s, ff_add(ff_sub(ff_from(f.s[6][s]), ff_mul(ddz, df_ff(odr, g.e[0], sp, sz))),
+                                          ff_mul(ddx, df_ff(odr, g.e[2], sp, 1))));
+    out[7] = rk_ff(rk, f.u0[7], s, ff_add(ff_sub(ff_from(f.s[7][s]), ff_mul(ddx, df_ff(odr, g.e[1], sp, 1))),
+                                          ff_mul(ddy, df_ff(odr, g.e[0], sp, sy))));
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
     const int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -694,7 +746,7 @@ int split3d_step(Sim *s, double dt)
             MLAU_CUDA(cudaMemcpyAsync(f.u0[v], f.s[v], sizeof(double) * G.n,
                                       cudaMemcpyDeviceToDevice, st));
     }
-    const dim3 cb(128), cg(blocks_for(G.nx, 128), G.ny, G.nz);
+    const dim3 cb(128), cg(blocks_for((long long)G.nx * G.ny, 128), G.nz);
     const dim3 ug(blocks_for(G.nx - 2 * G.ox, 128), G.ny - 2 * G.oy, G.nz - 2 * G.oz);
     const float gam = (float)s->gamma;
     for (int rk = 0; rk < s->nrk; rk++) {
@@ -704,7 +756,7 @@ int split3d_step(Sim *s, double dt)
         const double ra = t[rk][0], rb = t[rk][1];
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
-            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, s->gamma, (float)s->gamma);
+            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, host_ff(s->gamma - 1), (float)s->gamma);
             ks_aux<<<cg, cb, 0, st>>>(g, d);
         }
         {
@@ -720,9 +772,11 @@ int split3d_step(Sim *s, double dt)
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_UPDATE);
             const double c24 = lin_odr(s->odr) > 2 ? 1.0 / 24.0 : 1.0;
-            ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, ra, rb, (float)(dt / G.dx),
+            const RkFF rk{host_ff(ra), host_ff(rb), ra == 0.0 && rb == 1.0};
+            ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, rk, (float)(dt / G.dx),
                                          (float)(dt / G.dy), (float)(dt / G.dz),
-                                         dt / G.dx * c24, dt / G.dy * c24, dt / G.dz * c24);
+                                         host_ff(dt / G.dx * c24), host_ff(dt / G.dy * c24),
+                                         host_ff(dt / G.dz * c24));
         }
         MLAU_CUDA(cudaGetLastError());
     }
