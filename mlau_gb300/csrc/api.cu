@@ -188,7 +188,7 @@ int mlau_sim_destroy(mlau_sim *s)
     return MLAU_OK;
 }
 
-static int nvars(const Sim *s) { return 8; }
+static int nvars(const Sim *) { return 8; }
 
 int mlau_sim_upload(mlau_sim *s, const double *const *h)
 {
@@ -678,8 +678,7 @@ void mhd_fd_ct_3d(double *ro, double *mx, double *my, double *mz, double *en, do
         report("mhd_fd_ct_3d");
         return;
     }
-    static const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int *tx = dnxs ? dnxs : zero, *ty = dnys ? dnys : zero, *tz = dnzs ? dnzs : zero;
+    const int *tx = dnxs, *ty = dnys, *tz = dnzs;
     mlau_sim *c = get_ctx(3, nx, ny, nz, xoff, yoff, zoff, dx, dy, dz, gamma);
     double *h[8] = {ro, mx, my, mz, en, bx, by, bz};
     if (!c || mlau_sim_set_bc_3d(c, tx, ty, tz) != MLAU_OK || run_dropin(c, h, dt) != MLAU_OK)
@@ -696,8 +695,7 @@ static void dropin_2d(double *ro, double *mx, double *my, double *mz, double *en
                       int xoff, int yoff, double gamma, bool mpi)
 {
     std::lock_guard<std::mutex> lk(g_mu);
-    static const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int *tx = dnxs ? dnxs : zero, *ty = dnys ? dnys : zero;
+    const int *tx = dnxs, *ty = dnys;
     if (mpi)
         for (const int *t : {tx, ty}) {
             int nz = 0;
@@ -749,8 +747,7 @@ static int dropin_mrx(const char *who, double *const *h, const bool *back, doubl
         report(who);
         return MLAU_ERR_ARG;
     }
-    static const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int *tx = dnxs ? dnxs : zero, *ty = dnys ? dnys : zero;
+    const int *tx = dnxs, *ty = dnys;
     mlau_sim *c = get_ctx(2, nx, ny, 1, xoff, yoff, 0, dx, dy, 1.0, gamma);
     int rc = c ? mlau_sim_set_bc_2d(c, tx, ty) : MLAU_ERR_NOMEM;
     if (rc == MLAU_OK) rc = mlau_sim_upload(c, (const double *const *)h);
