@@ -82,6 +82,7 @@ struct SplitFields {
     int ntile[3][2] = {};   // tiles along the first two tile axes, per sweep
     int ntiles[3] = {};
     int nblocks[3] = {};    // persistent grid per sweep
+    int spec = 0;           // sweep instance: 0 run-time scheme, 1 WCNS4 + MLAU, 2 WCNS4 + LHLLD
     int *d_err = nullptr;   // set when a bounded wait gave up
 };
 
@@ -299,11 +300,17 @@ __device__ __forceinline__ void issue_tile(const SweepMaps &M, unsigned char *st
                     bar);
 }
 
-template <int D>
+// ODR / WHICH > 0 / >= 0 fix the reconstruction code and the solver at
+// compile time (the common schemes get their own instances: no run-time
+// dispatch and some 18 fewer registers per thread); 0 / -1 read them from
+// the arguments.
+template <int D, int ODR = 0, int WHICH = -1>
 __global__ void __launch_bounds__(SG<D>::TA *SG<D>::TB)
-ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr, int which, float gamma,
-         int n0, int n1, int ntiles, int *err)
+ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, int which_rt,
+         float gamma, int n0, int n1, int ntiles, int *err)
 {
+    const int odr = ODR ? ODR : odr_rt;
+    const int which = WHICH >= 0 ? WHICH : which_rt;
     constexpr int TA = SG<D>::TA, TB = SG<D>::TB, NB = box_elems<D>();
     constexpr unsigned STAGE = stage_bytes<D>();
     extern __shared__ unsigned char dyn_smem[];
@@ -582,6 +589,15 @@ void sweep_arrays(const SplitPtrs &g, int D, const void *q[NQ], const void *f[NF
     f[SF_DVU] = g.dv[dvu[D]];
 }
 
+// Opt a sweep instance into its dynamic shared memory and return how many of
+// its blocks fit on an SM.
+template <class K> int sweep_occupancy(K kernel, int threads, size_t dyn, int *per_sm)
+{
+    MLAU_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    MLAU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kernel, threads, dyn));
+    return MLAU_OK;
+}
+
 template <int D> int setup_sweep(Sim *s, SplitFields &sf)
 {
     const Geometry &G = s->g;
@@ -615,14 +631,17 @@ template <int D> int setup_sweep(Sim *s, SplitFields &sf)
     sf.ntile[D][0] = n0;
     sf.ntile[D][1] = n1;
     sf.ntiles[D] = n0 * n1 * n2;
-    const size_t dyn = sweep_dyn_smem<D>();
-    MLAU_CUDA(cudaFuncSetAttribute(ks_sweep<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)dyn));
-    int dev = 0, sms = 0, per_sm = 0;
+    int per_sm = 0;
+    const int ro = sf.spec == 1   ? sweep_occupancy(ks_sweep<D, 4, FLUX_MLAU>, SG<D>::TA * SG<D>::TB,
+                                              sweep_dyn_smem<D>(), &per_sm)
+             : sf.spec == 2 ? sweep_occupancy(ks_sweep<D, 4, FLUX_LHLLD>, SG<D>::TA * SG<D>::TB,
+                                              sweep_dyn_smem<D>(), &per_sm)
+                            : sweep_occupancy(ks_sweep<D>, SG<D>::TA * SG<D>::TB,
+                                              sweep_dyn_smem<D>(), &per_sm);
+    if (ro) return ro;
+    int dev = 0, sms = 0;
     MLAU_CUDA(cudaGetDevice(&dev));
     MLAU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    MLAU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks_sweep<D>,
-                                                            SG<D>::TA * SG<D>::TB, dyn));
     if (per_sm < 1) {
         set_error("FP32-split sweep %d does not fit on an SM", D);
         return MLAU_ERR_CUDA;
@@ -635,9 +654,19 @@ template <int D>
 void launch_sweep(Sim *s, SplitFields &sf, const Dims &d, float gam)
 {
     const dim3 b(SG<D>::TA, SG<D>::TB);
-    ks_sweep<D><<<sf.nblocks[D], b, sweep_dyn_smem<D>(), s->stream>>>(
-        sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1], sf.ntiles[D],
-        sf.d_err);
+    const size_t dyn = sweep_dyn_smem<D>();
+    if (sf.spec == 1)
+        ks_sweep<D, 4, FLUX_MLAU><<<sf.nblocks[D], b, dyn, s->stream>>>(
+            sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1],
+            sf.ntiles[D], sf.d_err);
+    else if (sf.spec == 2)
+        ks_sweep<D, 4, FLUX_LHLLD><<<sf.nblocks[D], b, dyn, s->stream>>>(
+            sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1],
+            sf.ntiles[D], sf.d_err);
+    else
+        ks_sweep<D><<<sf.nblocks[D], b, dyn, s->stream>>>(
+            sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1],
+            sf.ntiles[D], sf.d_err);
 }
 
 }  // namespace
@@ -706,6 +735,7 @@ int split3d_alloc(Sim *s)
     MLAU_CUDA(cudaMemset(sf.d_err, 0, sizeof(int)));
     // the sweeps read the arrays' ghost rows too: start from zeros
     for (int v = 0; v < 8; v++) MLAU_CUDA(cudaMemset(g.q[v], 0, sizeof(float2) * np));
+    sf.spec = (s->odr == 4 && s->flux == FLUX_MLAU) ? 1 : (s->odr == 4 && s->flux == FLUX_LHLLD) ? 2 : 0;
     int r2 = setup_sweep<0>(s, sf);
     if (!r2) r2 = setup_sweep<1>(s, sf);
     if (!r2) r2 = setup_sweep<2>(s, sf);
