@@ -241,8 +241,22 @@ def rel_l1(a, b, off=4):
 
 
 def run_e2e(args, R, st, meta, dt, M, prec):
+    """The same K steps through the reference-named driver with host arrays.
+    The host arrays are first touched, pinned and driven from the CPUs next to
+    this rank's GPU (its PCI root's local CPU list), so that on a multi-socket
+    host they sit on the GPU's own memory node, as a production caller would
+    place them; the affinity is restored afterwards."""
     n = args.n
-    host = {k: np.ascontiguousarray(st[k].copy()) for k in VARS}
+    cpus = M.local_cpus(R.local)
+    old_aff = os.sched_getaffinity(0) if cpus else None
+    if cpus:
+        try:
+            os.sched_setaffinity(0, cpus)
+        except OSError:
+            cpus = None
+    host = {k: np.empty_like(st[k]) for k in VARS}
+    for k in VARS:
+        host[k][...] = st[k]  # first touch from the local CPUs
     for a in host.values():
         M.pin(a)
     nz, ny, nx = host["ro"].shape
@@ -262,10 +276,15 @@ def run_e2e(args, R, st, meta, dt, M, prec):
     for a in host.values():
         M.unpin(a)
     M.release_dropin()
+    if old_aff:
+        os.sched_setaffinity(0, old_aff)
     bytes_per_step = sum(a.nbytes for a in host.values())
+    place = (f"host arrays on the GPU's local CPUs {min(cpus)}-{max(cpus)}" if cpus
+             else "host arrays where the process runs (GPU-local CPUs unknown)")
     return {"value": n ** 3 * args.steps * R.world / el, "unit": UNIT,
             "h2d_bytes_per_step": bytes_per_step, "d2h_bytes_per_step": bytes_per_step,
-            "path": "C ABI mhd_fd_ct_3d (reference signature), pinned host arrays"}
+            "path": "C ABI mhd_fd_ct_3d (reference signature), pinned host arrays",
+            "placement": place}
 
 
 def cpu_baseline(threads=None, n=96, steps=1):

@@ -362,6 +362,10 @@ int mlau_pin_host(void *ptr, long long bytes);
 int mlau_unpin_host(void *ptr);
 /* Select the CUDA device used by this host thread's later calls. */
 int mlau_set_device(int device);
+/* PCI bus id of a device ("domain:bus:device.function"), e.g. to find the
+ * host CPUs and memory node next to it, where host arrays that cross the
+ * link every step belong. */
+int mlau_device_pci_bus_id(int device, char *buf, int len);
 
 #ifdef __cplusplus
 }

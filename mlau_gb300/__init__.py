@@ -73,6 +73,7 @@ def _bind(lib):
     lib.mlau_pin_host.argtypes = [vp, C.c_longlong]
     lib.mlau_unpin_host.argtypes = [vp]
     lib.mlau_set_device.argtypes = [i]
+    lib.mlau_device_pci_bus_id.argtypes = [i, C.c_char_p, i]
     cp = C.c_char_p
     lib.mlau_sim_bkup_save.argtypes = [vp, cp, i, i, d, d, d, i]
     lib.mlau_sim_bkup_load.argtypes = [vp, cp, C.POINTER(i), C.POINTER(i), pd, pd, pd, i]
@@ -218,6 +219,33 @@ def measure_fma_peaks():
 
 def set_device(dev: int):
     _check(lib().mlau_set_device(dev))
+
+
+def local_cpus(dev: int = 0):
+    """The host CPUs attached to a device's PCI root (Linux sysfs), or None
+    where that is not known.  Host arrays first touched by a thread on these
+    CPUs sit on the device's own memory node, which is what keeps per-step
+    host<->device copies at the link's full speed on multi-socket hosts."""
+    buf = C.create_string_buffer(64)
+    if lib().mlau_device_pci_bus_id(dev, buf, 64) != 0:
+        return None
+    parts = buf.value.decode().lower().split(":")
+    if len(parts) != 3:
+        return None
+    bus = f"{int(parts[0], 16):04x}:{parts[1]}:{parts[2]}"
+    try:
+        with open(f"/sys/bus/pci/devices/{bus}/local_cpulist") as fh:
+            spec = fh.read().strip()
+    except OSError:
+        return None
+    cpus = set()
+    for part in spec.split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        elif part:
+            cpus.add(int(part))
+    return cpus or None
 
 
 def pin(arr: np.ndarray):

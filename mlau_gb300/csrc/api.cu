@@ -495,6 +495,13 @@ int mlau_set_device(int dev)
     return MLAU_OK;
 }
 
+int mlau_device_pci_bus_id(int dev, char *buf, int len)
+{
+    if (!buf || len < 16) { set_error("buffer too small"); return MLAU_ERR_ARG; }
+    MLAU_CUDA(cudaDeviceGetPCIBusId(buf, len, dev));
+    return MLAU_OK;
+}
+
 int mlau_unpin_host(void *p)
 {
     MLAU_CUDA(cudaHostUnregister(p));
