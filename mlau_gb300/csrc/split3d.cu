@@ -134,7 +134,7 @@ __device__ __forceinline__ ff face2cen_ff(int odr, const double *b, long long w,
 }
 
 __global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, int save_u0)
 {
     int i, j, k;
     if (!plane_cell(d, i, j, k)) return;
@@ -169,6 +169,11 @@ ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f)
     g.bf[0][sp] = to_f32(f.s[5][s]);
     g.bf[1][sp] = to_f32(f.s[6][s]);
     g.bf[2][sp] = to_f32(f.s[7][s]);
+    // the first stage keeps U^n for the later stages' RK combine (this
+    // kernel has loaded every state value of the cell already)
+    if (save_u0)
+#pragma unroll
+        for (int v = 0; v < 8; v++) f.u0[v][s] = f.s[v][s];
     g.m2[sp] = v2 / (gamma_f * (pr2.x + pr2.y) * irof);
 }
 
@@ -770,12 +775,6 @@ int split3d_step(Sim *s, double dt)
     SplitPtrs &g = sf.p;
     cudaStream_t st = s->stream;
     const Dims d{G.nx, G.ny, G.nz, G.ox, G.oy, G.oz, sf.px};
-    {
-        TimedLaunch tl(&s->timer, KK_COPY);
-        for (int v = 0; v < 8; v++)
-            MLAU_CUDA(cudaMemcpyAsync(f.u0[v], f.s[v], sizeof(double) * G.n,
-                                      cudaMemcpyDeviceToDevice, st));
-    }
     const dim3 cb(128), cg(blocks_for((long long)G.nx * G.ny, 128), G.nz);
     const dim3 ug(blocks_for(G.nx - 2 * G.ox, 128), G.ny - 2 * G.oy, G.nz - 2 * G.oz);
     const float gam = (float)s->gamma;
@@ -786,7 +785,8 @@ int split3d_step(Sim *s, double dt)
         const double ra = t[rk][0], rb = t[rk][1];
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
-            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, host_ff(s->gamma - 1), (float)s->gamma);
+            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, host_ff(s->gamma - 1), (float)s->gamma,
+                                       rk == 0);
             ks_aux<<<cg, cb, 0, st>>>(g, d);
         }
         {
