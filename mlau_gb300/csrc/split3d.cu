@@ -47,6 +47,7 @@
 #include "tma.cuh"
 #include "split_conv.cuh"
 #include "ff.cuh"
+#include "point_x2.cuh"
 
 #include <algorithm>
 
@@ -69,7 +70,7 @@ struct SplitPtrs {
     float *bf[3];    // face-centred bx, by, bz rounded to FP32
     float *F[3][7];
     float *FC[3][2];
-    double *e[3];    // edge EMFs (FP32 values held in FP64 for the CT curl)
+    float *e[3];     // edge EMFs
     float *m2;
     float *ct[3];
     float *dv[3];
@@ -233,12 +234,12 @@ template <> struct SG<0> {
     static constexpr int BX = 40, BY = 4, BZ = 1;
 };
 template <> struct SG<1> {
-    static constexpr int TA = 16, TB = 16, T = 16;
-    static constexpr int BX = 16, BY = 20, BZ = 1;
+    static constexpr int TA = 8, TB = 16, T = 16;
+    static constexpr int BX = 8, BY = 20, BZ = 1;
 };
 template <> struct SG<2> {
-    static constexpr int TA = 16, TB = 16, T = 16;
-    static constexpr int BX = 16, BY = 1, BZ = 20;
+    static constexpr int TA = 8, TB = 16, T = 16;
+    static constexpr int BX = 8, BY = 1, BZ = 20;
 };
 template <int D> __host__ __device__ constexpr int box_elems() { return SG<D>::BX * SG<D>::BY * SG<D>::BZ; }
 template <int D> __host__ __device__ constexpr unsigned stage_bytes()
@@ -305,12 +306,148 @@ __device__ __forceinline__ void issue_tile(const SweepMaps &M, unsigned char *st
                     bar);
 }
 
+// Per-cell results of a sweep tile in shared memory: sl / sr - the face
+// perturbations at the cell's right / left face plus the two central CT parts;
+// sb - the cell-centre state as (hi, lo).
+template <int D> struct CellSmem {
+    float (&sl)[9][SG<D>::TB][SG<D>::TA];
+    float (&sr)[9][SG<D>::TB][SG<D>::TA];
+    float2 (&sb)[7][SG<D>::TB][SG<D>::TA];
+};
+
+// Reconstruction of one cell, any scheme: characteristic projection of the
+// stencil perturbations, the scheme's face interpolation, back-projection;
+// the central parts lin(bt vn) - bn_face lin(vt) of the two tangential B
+// fluxes.
+template <int D>
+__device__ __forceinline__ void rec_cell(const float2 *Q, const float *Fs, const TileAt &a, int ta,
+                                         int tb, int odr, float gamma, const CellSmem<D> &c)
+{
+    constexpr int NB = box_elems<D>();
+    auto QI = [&](int n, int m) { return Q[n * NB + bidx<D>(a, ta, tb, m)]; };
+    auto FI = [&](int n, int m) { return Fs[n * NB + bidx<D>(a, ta, tb, m)]; };
+    float dq[7][5], qc[7];
+    unsigned zero = 0;
+#pragma unroll
+    for (int n = 0; n < 7; n++) {
+        float2 h[5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) h[m] = QI(n, m);
+        qc[n] = h[2].x + h[2].y;
+        bool z = true;
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            dq[n][m] = (h[m].x - h[2].x) + (h[m].y - h[2].y);
+            z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
+        }
+        if (z) zero |= 1u << n;
+        c.sb[n][tb][ta] = h[2];
+    }
+    float ul[7], ur[7];
+    const float2 bn2 = QI(SQ_BN, 2);
+    const float bnc = bn2.x + bn2.y;
+    const float mm = fmaxf(FI(SF_M2, 1), fmaxf(FI(SF_M2, 2), FI(SF_M2, 3)));
+    if (mm >= 1.0f) reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
+    else reconst_alfven_core(odr, dq, qc, bnc, gamma, ul, ur);
+#pragma unroll
+    for (int n = 1; n <= 5; n++)
+        if (zero & (1u << n)) { ul[n] = 0.f; ur[n] = 0.f; }
+#pragma unroll
+    for (int n = 0; n < 7; n++) { c.sl[n][tb][ta] = ul[n]; c.sr[n][tb][ta] = ur[n]; }
+    const float bl = FI(SF_BF, 3), br = FI(SF_BF, 2);
+#pragma unroll
+    for (int tt = 0; tt < 2; tt++) {
+        const int kb = 4 + tt, kv = 2 + tt;
+        const float a0 = (qc[kb]) * (qc[1]);
+        float da[5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) da[m] = (qc[kb] + dq[kb][m]) * (qc[1] + dq[1][m]) - a0;
+        const float al = a0 + lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
+        const float ar = a0 + lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
+        const float vl = qc[kv] + lin_l(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
+        const float vr = qc[kv] + lin_r(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
+        c.sl[7 + tt][tb][ta] = al - bl * vl;
+        c.sr[7 + tt][tb][ta] = ar - br * vr;
+    }
+}
+
+// The same for WCNS4, on packed FP32x2 pairs (point_x2.cuh): the stencil
+// perturbations as outer (f0, f4) and inner (f1, f3) pairs - the centre one
+// is zero - and the face values as (left, right) pairs.  The central CT parts
+// take the product perturbation in expanded form, (qb + db)(qv + dv) - qb qv
+// = db (qv + dv) + qb dv, which keeps it to FP32 relative accuracy.
+template <int D>
+__device__ __forceinline__ void rec_cell_wcns4(const float2 *Q, const float *Fs, const TileAt &a,
+                                               int ta, int tb, int odr, float gamma,
+                                               const CellSmem<D> &c)
+{
+    constexpr int NB = box_elems<D>();
+    auto QI = [&](int n, int m) { return Q[n * NB + bidx<D>(a, ta, tb, m)]; };
+    auto FI = [&](int n, int m) { return Fs[n * NB + bidx<D>(a, ta, tb, m)]; };
+    float2 O[7], I[7];
+    float qc[7];
+    unsigned zero = 0;
+#pragma unroll
+    for (int n = 0; n < 7; n++) {
+        float2 h[5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) h[m] = QI(n, m);
+        qc[n] = h[2].x + h[2].y;
+        float dqm[5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            if (m == 2) continue;
+            const float2 t = x2sub(h[m], h[2]);  // (hi_m - hi_c, lo_m - lo_c)
+            dqm[m] = t.x + t.y;
+        }
+        O[n] = make_float2(dqm[0], dqm[4]);
+        I[n] = make_float2(dqm[1], dqm[3]);
+        bool z = true;
+#pragma unroll
+        for (int m = 0; m < 5; m++) z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
+        if (z) zero |= 1u << n;
+        c.sb[n][tb][ta] = h[2];
+    }
+    const float2 bn2 = QI(SQ_BN, 2);
+    const float bnc = bn2.x + bn2.y;
+    const float mm = fmaxf(FI(SF_M2, 1), fmaxf(FI(SF_M2, 2), FI(SF_M2, 3)));
+    float2 LR[7];
+    if (mm >= 1.0f) {
+        float dq[7][5], ul[7], ur[7];
+#pragma unroll
+        for (int n = 0; n < 7; n++) {
+            dq[n][0] = O[n].x; dq[n][1] = I[n].x; dq[n][2] = 0.f; dq[n][3] = I[n].y; dq[n][4] = O[n].y;
+        }
+        reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
+#pragma unroll
+        for (int n = 0; n < 7; n++) LR[n] = make_float2(ul[n], ur[n]);
+    } else {
+        reconst_alfven_wcns4_x2(O, I, qc, bnc, gamma, LR);
+    }
+#pragma unroll
+    for (int n = 1; n <= 5; n++)
+        if (zero & (1u << n)) LR[n] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int n = 0; n < 7; n++) { c.sl[n][tb][ta] = LR[n].x; c.sr[n][tb][ta] = LR[n].y; }
+    const float bl = FI(SF_BF, 3), br = FI(SF_BF, 2);
+#pragma unroll
+    for (int tt = 0; tt < 2; tt++) {
+        const int kb = 4 + tt, kv = 2 + tt;
+        const float a0 = qc[kb] * qc[1];
+        const float2 dao = x2fma(O[kb], x2add(x2k(qc[1]), O[1]), x2mul(x2k(qc[kb]), O[1]));
+        const float2 dai = x2fma(I[kb], x2add(x2k(qc[1]), I[1]), x2mul(x2k(qc[kb]), I[1]));
+        const float2 A = lin4_pert_x2(dao, dai), V = lin4_pert_x2(O[kv], I[kv]);
+        c.sl[7 + tt][tb][ta] = (a0 + A.x) - bl * (qc[kv] + V.x);
+        c.sr[7 + tt][tb][ta] = (a0 + A.y) - br * (qc[kv] + V.y);
+    }
+}
+
 // ODR / WHICH > 0 / >= 0 fix the reconstruction code and the solver at
 // compile time (the common schemes get their own instances: no run-time
 // dispatch and some 18 fewer registers per thread); 0 / -1 read them from
 // the arguments.
 template <int D, int ODR = 0, int WHICH = -1>
-__global__ void __launch_bounds__(SG<D>::TA *SG<D>::TB)
+__global__ void __launch_bounds__(SG<D>::TA *SG<D>::TB, ODR ? 5 : 1)
 ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, int which_rt,
          float gamma, int n0, int n1, int ntiles, int *err)
 {
@@ -368,51 +505,9 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
         auto FI = [&](int n, int m) { return Fs[n * NB + bidx<D>(a, ta, tb, m)]; };
 
         if (do_rec) {
-            float dq[7][5], qc[7];
-            unsigned zero = 0;
-#pragma unroll
-            for (int n = 0; n < 7; n++) {
-                float2 h[5];
-#pragma unroll
-                for (int m = 0; m < 5; m++) h[m] = QI(n, m);
-                qc[n] = h[2].x + h[2].y;
-                bool z = true;
-#pragma unroll
-                for (int m = 0; m < 5; m++) {
-                    dq[n][m] = (h[m].x - h[2].x) + (h[m].y - h[2].y);
-                    z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
-                }
-                if (z) zero |= 1u << n;
-                sb[n][tb][ta] = h[2];
-            }
-            float ul[7], ur[7];
-            const float2 bn2 = QI(SQ_BN, 2);
-            const float bnc = bn2.x + bn2.y;
-            const float mm = fmaxf(FI(SF_M2, 1), fmaxf(FI(SF_M2, 2), FI(SF_M2, 3)));
-            if (mm >= 1.0f) reconst_full_core(odr, dq, qc, bnc, gamma, ul, ur);
-            else reconst_alfven_core(odr, dq, qc, bnc, gamma, ul, ur);
-#pragma unroll
-            for (int n = 1; n <= 5; n++)
-                if (zero & (1u << n)) { ul[n] = 0.f; ur[n] = 0.f; }
-#pragma unroll
-            for (int n = 0; n < 7; n++) { sl[n][tb][ta] = ul[n]; sr[n][tb][ta] = ur[n]; }
-            // central parts of the two tangential B fluxes: lin(bt vn) - bn_face lin(vt)
-            const float bl = FI(SF_BF, 3), br = FI(SF_BF, 2);
-#pragma unroll
-            for (int tt = 0; tt < 2; tt++) {
-                const int kb = 4 + tt, kv = 2 + tt;
-                const float a0 = (qc[kb]) * (qc[1]);
-                float da[5];
-#pragma unroll
-                for (int m = 0; m < 5; m++)
-                    da[m] = (qc[kb] + dq[kb][m]) * (qc[1] + dq[1][m]) - a0;
-                const float al = a0 + lin_l(odr, da[0], da[1], da[2], da[3], da[4]);
-                const float ar = a0 + lin_r(odr, da[0], da[1], da[2], da[3], da[4]);
-                const float vl = qc[kv] + lin_l(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
-                const float vr = qc[kv] + lin_r(odr, dq[kv][0], dq[kv][1], dq[kv][2], dq[kv][3], dq[kv][4]);
-                sl[7 + tt][tb][ta] = al - bl * vl;
-                sr[7 + tt][tb][ta] = ar - br * vr;
-            }
+            const CellSmem<D> cs{sl, sr, sb};
+            if constexpr (ODR == 4) rec_cell_wcns4<D>(Q, Fs, a, ta, tb, odr, gamma, cs);
+            else rec_cell<D>(Q, Fs, a, ta, tb, odr, gamma, cs);
         }
         __syncthreads();
 
@@ -487,31 +582,31 @@ __global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr)
         ey = emf_part32(g.F[0][5], g.FC[0][1], w, 0.5f, c, sz, odr)
              + emf_part32(g.F[2][4], g.FC[2][0], 1.f - w, -0.5f, c, 1, odr);
     }
-    g.e[0][c] = to_f64(ex);
-    g.e[1][c] = to_f64(ey);
-    g.e[2][c] = to_f64(ez);
+    g.e[0][c] = ex;
+    g.e[1][c] = ey;
+    g.e[2][c] = ez;
 }
 
 // --- RK combine + CT curl ------------------------------------------------------
 // The flux divergence dt/dx dF + dt/dy dG + dt/dz dH is formed in FP32 (each
 // difference of neighbouring FP32 fluxes is exact when they share sign and
-// magnitude) and accumulated into the FP64 state in FP64.
-__device__ __forceinline__ float df32(int odr, const float *f, long long s, long long st)
-{
-    return fdiff(odr, f[s - st], f[s], f[s + st], f[s + 2 * st]);
-}
+// magnitude) and accumulated into the state in float-float.
+//
+// The kernel streams some 60 flux values, 24 edge EMFs and 16 state values
+// per cell with little arithmetic between them, so it is bound by memory
+// latency unless the loads are in flight together: every value is read into
+// registers first (read-only data through the non-coherent path), and the
+// arithmetic follows.
 
-// Float-float difference of the (FP32-valued) edge EMFs along one axis,
-// without the 1/24 of the 4th-order stencil (folded into dt/dx by the
-// caller): the differences of two floats are exact as float-float, and so is
-// 27 times one, so the discrete divergence of the curl cancels to the
-// float-float round-off.
-__device__ __forceinline__ ff df_ff(int odr, const double *f, long long s, long long st)
+// Float-float difference of the FP32 edge EMFs f0..f3 along one axis, without
+// the 1/24 of the 4th-order stencil (folded into dt/dx by the caller): the
+// differences of two floats are exact as float-float, and so is 27 times one,
+// so the discrete divergence of the curl cancels to the float-float
+// round-off.
+__device__ __forceinline__ ff df_ff(int odr, const float e[4])
 {
-    const float f1 = to_f32(f[s]), f2 = to_f32(f[s + st]);
-    if (lin_odr(odr) <= 2) return ff_two_sum(f2, -f1);
-    const float f0 = to_f32(f[s - st]), f3 = to_f32(f[s + 2 * st]);
-    return ff_sub(ff_mul_f(ff_two_sum(f2, -f1), 27.0f), ff_two_sum(f3, -f0));
+    if (lin_odr(odr) <= 2) return ff_two_sum(e[2], -e[1]);
+    return ff_sub(ff_mul_f(ff_two_sum(e[2], -e[1]), 27.0f), ff_two_sum(e[3], -e[0]));
 }
 
 // The RK combine ra u0 + rb u in float-float (ra = 0, rb = 1 at the first stage).
@@ -519,13 +614,20 @@ struct RkFF {
     float2 ra, rb;
     int first;
 };
-__device__ __forceinline__ double rk_ff(const RkFF &c, const double *u0, long long s, ff u)
+__device__ __forceinline__ double rk_ff(const RkFF &c, double u0, ff u)
 {
     if (c.first) return ff_to_double(u);
-    return ff_to_double(ff_add(ff_mul({c.ra.x, c.ra.y}, ff_from(u0[s])), ff_mul({c.rb.x, c.rb.y}, u)));
+    return ff_to_double(ff_add(ff_mul({c.ra.x, c.ra.y}, ff_from(u0)), ff_mul({c.rb.x, c.rb.y}, u)));
 }
 
-__global__ void __launch_bounds__(256)
+// Stencil f[s - st], f[s], f[s + st], f[s + 2 st] of a read-only array.
+__device__ __forceinline__ void ld4(float v[4], const float *f, long long s, long long st)
+{
+#pragma unroll
+    for (int m = 0; m < 4; m++) v[m] = __ldg(f + s + (m - 1) * st);
+}
+
+__global__ void __launch_bounds__(128)
 ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, float dtdx, float dtdy,
           float dtdz, float2 ddx2, float2 ddy2, float2 ddz2)
 {
@@ -535,26 +637,48 @@ ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, float dtdx, floa
     const long long sy = d.px, sz = d.px * d.ny;  // scratch strides
     const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
     const int cX[5] = {0, 1, 2, 3, 6}, cY[5] = {0, 3, 1, 2, 6}, cZ[5] = {0, 2, 3, 1, 6};
+    // loads
+    float fx[5][4], fy[5][4], fz[5][4];
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        ld4(fx[v], g.F[0][cX[v]], sp, 1);
+        ld4(fy[v], g.F[1][cY[v]], sp, sy);
+        ld4(fz[v], g.F[2][cZ[v]], sp, sz);
+    }
+    float ezy[4], eyz[4], exz[4], ezx[4], eyx[4], exy[4];
+    ld4(ezy, g.e[2], sp, sy);
+    ld4(eyz, g.e[1], sp, sz);
+    ld4(exz, g.e[0], sp, sz);
+    ld4(ezx, g.e[2], sp, 1);
+    ld4(eyx, g.e[1], sp, 1);
+    ld4(exy, g.e[0], sp, sy);
+    double u[8], u0[8];
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+        u[v] = f.s[v][s];
+        u0[v] = rk.first ? 0.0 : __ldg(f.u0[v] + s);
+    }
+    // arithmetic
     double out[8];
 #pragma unroll
     for (int v = 0; v < 5; v++) {
-        const float div = dtdx * df32(odr, g.F[0][cX[v]], sp, 1) + dtdy * df32(odr, g.F[1][cY[v]], sp, sy)
-                          + dtdz * df32(odr, g.F[2][cZ[v]], sp, sz);
+        const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
+                          + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
+                          + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
         // the first stage is u - div: one FP64 addition beats its float-float form
-        out[v] = rk.first ? f.s[v][s] - to_f64(div)
-                          : rk_ff(rk, f.u0[v], s, ff_add_f(ff_from(f.s[v][s]), -div));
+        out[v] = rk.first ? u[v] - to_f64(div) : rk_ff(rk, u0[v], ff_add_f(ff_from(u[v]), -div));
     }
     // CT curl in float-float: the differences of the FP32 edge EMFs are
     // exact, so the discrete divergence of the B increment cancels to the
     // float-float round-off (in FP32, 27*(E2-E1) alone would need more than
     // 24 bits).  ddx2 etc. carry the stencil's 1/24 when odr > 2.
     const ff ddx = {ddx2.x, ddx2.y}, ddy = {ddy2.x, ddy2.y}, ddz = {ddz2.x, ddz2.y};
-    out[5] = rk_ff(rk, f.u0[5], s, ff_add(ff_sub(ff_from(f.s[5][s]), ff_mul(ddy, df_ff(odr, g.e[2], sp, sy))),
-                                          ff_mul(ddz, df_ff(odr, g.e[1], sp, sz))));
-    out[6] = rk_ff(rk, f.u0[6], s, ff_add(ff_sub(ff_from(f.s[6][s]), ff_mul(ddz, df_ff(odr, g.e[0], sp, sz))),
-                                          ff_mul(ddx, df_ff(odr, g.e[2], sp, 1))));
-    out[7] = rk_ff(rk, f.u0[7], s, ff_add(ff_sub(ff_from(f.s[7][s]), ff_mul(ddx, df_ff(odr, g.e[1], sp, 1))),
-                                          ff_mul(ddy, df_ff(odr, g.e[0], sp, sy))));
+    out[5] = rk_ff(rk, u0[5], ff_add(ff_sub(ff_from(u[5]), ff_mul(ddy, df_ff(odr, ezy))),
+                                     ff_mul(ddz, df_ff(odr, eyz))));
+    out[6] = rk_ff(rk, u0[6], ff_add(ff_sub(ff_from(u[6]), ff_mul(ddz, df_ff(odr, exz))),
+                                     ff_mul(ddx, df_ff(odr, ezx))));
+    out[7] = rk_ff(rk, u0[7], ff_add(ff_sub(ff_from(u[7]), ff_mul(ddx, df_ff(odr, eyx))),
+                                     ff_mul(ddy, df_ff(odr, exy))));
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
     const int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -730,7 +854,7 @@ int split3d_alloc(Sim *s)
     for (int D = 0; D < 3; D++) {
         for (int v = 0; v < 7; v++) rc |= falloc(s, &g.F[D][v], np);
         rc |= falloc(s, &g.FC[D][0], np) | falloc(s, &g.FC[D][1], np);
-        rc |= dalloc(s, &g.e[D], np) | falloc(s, &g.ct[D], np) | falloc(s, &g.dv[D], np);
+        rc |= falloc(s, &g.e[D], np) | falloc(s, &g.ct[D], np) | falloc(s, &g.dv[D], np);
     }
     rc |= falloc(s, &g.m2, np);
     double *flag = nullptr;
