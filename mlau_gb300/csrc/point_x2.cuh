@@ -19,6 +19,8 @@
 
 #include <cuda_runtime.h>
 
+#include "point.cuh"
+
 namespace mlau {
 
 __device__ __forceinline__ float2 x2k(float c) { return make_float2(c, c); }
@@ -111,6 +113,134 @@ __device__ __forceinline__ void reconst_alfven_wcns4_x2(const float2 O[7], const
     LR[4] = x2mul(x2k(0.5f), x2sub(W[3], W[4]));
     LR[5] = x2mul(x2k(0.5f), x2sub(W[5], W[6]));
     LR[6] = x2fma(x2k(-bz), LR[5], x2fma(x2k(-by), LR[4], W[2]));
+}
+
+// calc_flux_mlau (include/mhd_flux.h:26-213) in its split-jump form
+// (flux_mlau<float, true>), with the left and right states as the lanes of
+// the pairs P[n] = (L[n], R[n]), n = ro, vn, vt, vu, bt, bu, pr.  The
+// per-side quantities - energies, enthalpies, fast and "cc" speeds, the Mach
+// polynomials, the star-state corrections - run as packed operations; the
+// right side's Mach polynomials are those of the left side at -Mn, so both
+// come from one evaluation at (Mn_l, -Mn_r).
+__device__ __forceinline__ void flux_mlau_x2(const float2 P[7], float bnc, float gamma, float dv0,
+                                             float dv1, float f[7], float jp, float jv)
+{
+    const float EPS = 1e-8f;
+    const float2 ro = P[0], vn = P[1], vt = P[2], vu = P[3], bt = P[4], bu = P[5], pr = P[6];
+    const float gm1i = 1.f / (gamma - 1.f);
+    const float bnc2 = bnc * bnc;
+    const float sgn = (bnc > 0.f) ? 1.f : -1.f;
+    const float bnca = sgn * bnc;
+    const float2 roi = make_float2(1.f / ro.x, 1.f / ro.y);
+    const float2 v2 = x2fma(vu, vu, x2fma(vt, vt, x2mul(vn, vn)));
+    const float2 pm = x2mul(x2k(0.5f), x2fma(bt, bt, x2mul(bu, bu)));
+    const float2 pt = x2add(pr, pm);
+    const float2 en = x2fma(x2mul(x2k(0.5f), ro), v2, x2fma(x2k(gm1i), pr, pm));
+    const float2 hn = x2mul(x2add(en, pt), roi);
+    const float2 c2 = x2mul(x2mul(x2k(gamma), pr), roi);
+    const float2 ca2 = x2mul(x2k(bnc2), roi);
+    const float2 pm2 = x2mul(x2mul(x2k(2.f), pm), roi);
+    float2 cb2 = x2add(x2add(c2, ca2), pm2);
+    float2 dsc = x2fma(cb2, cb2, x2mul(x2mul(x2k(-4.f), c2), ca2));
+    const float2 cf2 = x2mul(x2k(0.5f), x2add(cb2, make_float2(sqrtf(fabsf(dsc.x)), sqrtf(fabsf(dsc.y)))));
+    cb2 = x2add(x2add(v2, ca2), pm2);
+    dsc = x2fma(cb2, cb2, x2mul(x2mul(x2k(-4.f), v2), ca2));
+    const float2 cc2 = x2mul(x2k(0.5f), x2add(cb2, make_float2(sqrtf(fabsf(dsc.x)), sqrtf(fabsf(dsc.y)))));
+    const float cmax = sqrtf(vmax(cf2.x, cf2.y));
+    const float cfn = cmax;
+    const float cfni = 1.f / cfn;
+    const float sl = vmin(0.f, vmin(vn.x, vn.y) - cmax);
+    const float sr = vmax(0.f, vmax(vn.x, vn.y) + cmax);
+    float theta = vmin(1.f, (cfn - vmin(dv0, 0.f)) / (cfn - vmin(dv1, 0.f)));
+    theta *= theta;
+    theta *= theta;
+    const float alpha = 0.1875f, beta = 0.125f;
+    // Mach polynomials at m = (Mn_l, -Mn_r): lanes (bfl, bfr), (ffl, -ffr)
+    const float2 m = x2mul(vn, make_float2(cfni, -cfni));
+    const float2 mp1 = x2add(m, x2k(1.f));
+    const float2 m2m1 = x2fma(m, m, x2k(-1.f));
+    const float2 mp1s = x2mul(mp1, mp1), m2m1s = x2mul(m2m1, m2m1);
+    const float2 bsub = x2fma(x2mul(x2k(alpha), m), m2m1s,
+                              x2mul(x2mul(x2k(0.25f), mp1s), x2sub(x2k(2.f), m)));
+    const float2 fsub = x2fma(x2k(beta), m2m1s, x2mul(x2k(0.25f), mp1s));
+    // supersonic side (|Mn| > 1): bf = 1 moving away from the face, else 0; ff = bf Mn
+    const bool supl = fabsf(m.x) > 1.f, supr = fabsf(m.y) > 1.f;
+    const float bfl = supl ? (m.x > 0.f ? 1.f : 0.f) : bsub.x;
+    const float bfr = supr ? (m.y > 0.f ? 1.f : 0.f) : bsub.y;
+    const float ffl = supl ? bfl * m.x : fsub.x;
+    const float ffr = supr ? bfr * (-m.y) : -fsub.y;
+    const float mnc = ffl + ffr;
+    float mflux = mnc * cfn;
+    mflux -= vmax(1.f - fabsf(mnc), 0.f) * theta * cfni * jp / (ro.x + ro.y);
+    const float dir = (mflux > 0.f) ? 1.f : -1.f;
+    const float dirl = 0.5f * (1.f + dir);
+    const float dirr = 1.f - dirl;
+    mflux *= (dirl * ro.x + dirr * ro.y);
+    const float mfl = mflux * dirl;
+    const float mfr = mflux - mfl;
+    float ptot = bfl * pt.x + bfr * pt.y;
+    const float cfmod = sqrtf(vmax(cc2.x, cc2.y));
+    ptot -= 0.25f * bfl * bfr * (ro.x + ro.y) * cfmod * jv;
+    ptot -= 0.5f * (1.f - cfmod * cfni) * (bfl + bfr - 1.f) * (pt.x + pt.y);
+    const float2 sv = x2sub(make_float2(sl, sr), vn);  // (sl - vnl, sr - vnr)
+    const float snc = dirl * sl + dirr * sr;
+    const float vndnm = mflux + dirl * ro.x * sv.x + dirr * ro.y * sv.y;
+    const float vnc = ((fabsf(vndnm) > EPS) && (snc != 0.f)) ? (mflux * snc / vndnm)
+                                                             : (dirl * vn.x + dirr * vn.y);
+    const float2 svc = x2sub(make_float2(sl, sr), x2k(vnc));  // (sl - vnc, sr - vnc)
+    const float2 svci = make_float2(1.f / svc.x, 1.f / svc.y);
+    const float2 rhd = x2fma(x2mul(ro, sv), svc, x2k(-bnc2));
+    const float2 gq = x2sub(x2k(vnc), vn);
+    const float2 g = make_float2(fabsf(rhd.x) > EPS ? gq.x / rhd.x : 0.f,
+                                 fabsf(rhd.y) > EPS ? gq.y / rhd.y : 0.f);
+    const float2 dvt = x2mul(x2mul(x2k(-bnc), bt), g), dvu = x2mul(x2mul(x2k(-bnc), bu), g);
+    const float2 gs = x2mul(g, svci);
+    const float2 dbt = x2mul(x2mul(x2k(bnc2), bt), gs), dbu = x2mul(x2mul(x2k(bnc2), bu), gs);
+    const float2 cmp = x2mul(sv, svci);
+    const float2 ro2 = x2mul(ro, cmp);
+    const float srol = sqrtf(ro2.x), sror = sqrtf(ro2.y);
+    const float2 vt2 = x2add(dvt, vt), vu2 = x2add(dvu, vu);
+    const float2 bt2 = x2fma(bt, cmp, dbt), bu2 = x2fma(bu, cmp, dbu);
+    const float sroi = 1.f / (srol + sror);
+    const float srollri = srol * sroi, srorlri = sror * sroi;
+    const float bnflb = sgn * vmin(vmax(0.f, srollri * (bnca + sror * vnc)), bnca);
+    const float bnfrb = sgn * vmin(vmax(0.f, srorlri * (bnca - srol * vnc)), bnca);
+    const float bnflv = sgn * vmin(vmax(0.f, srorlri * (bnca + mflux / sror)), bnca);
+    const float bnfrv = sgn * vmin(vmax(0.f, srollri * (bnca - mflux / srol)), bnca);
+    const float bnsrv = vmax(bnca - dir * vnc * (dirl * srol + dirr * sror), 0.f);
+    const float ccb = sroi * bnsrv;
+    const float ccv = srol * sror * ccb;
+    float bnvt = bnflb * vt2.x + bnfrb * vt2.y + ccb * (bt2.y - bt2.x);
+    float bnvu = bnflb * vu2.x + bnfrb * vu2.y + ccb * (bu2.y - bu2.x);
+    float bnbt = bnflv * bt2.x + bnfrv * bt2.y + ccv * (vt2.y - vt2.x);
+    float bnbu = bnflv * bu2.x + bnfrv * bu2.y + ccv * (vu2.y - vu2.x);
+    bnvt -= vnc * (dirl * dbt.x + dirr * dbt.y);
+    bnvu -= vnc * (dirl * dbu.x + dirr * dbu.y);
+    bnbt -= mflux * (dirl * dvt.x + dirr * dvt.y);
+    bnbu -= mflux * (dirl * dvu.x + dirr * dvu.y);
+    const float2 mf = make_float2(mfl, mfr);
+    f[0] = mflux;
+    const float2 a1 = x2mul(mf, vn), a2 = x2mul(mf, vt), a3 = x2mul(mf, vu);
+    const float2 a4 = x2mul(x2mul(mf, bt), roi), a5 = x2mul(x2mul(mf, bu), roi);
+    f[1] = a1.x + a1.y + ptot - 0.5f * bnc2;
+    f[2] = a2.x + a2.y - bnbt;
+    f[3] = a3.x + a3.y - bnbu;
+    f[4] = a4.x + a4.y - bnvt;
+    f[5] = a5.x + a5.y - bnvu;
+    const float2 vb1s = x2fma(vt, bt, x2mul(vu, bu)), vb2s = x2fma(vt2, bt2, x2mul(vu2, bu2));
+    const float vb1 = dirl * vb1s.x + dirr * vb1s.y;
+    const float vb2 = dirl * vb2s.x + dirr * vb2s.y;
+    float rv2b2 = (mflux * vnc - bnc2);
+    rv2b2 *= rv2b2;
+    float vb3 = 0.f;
+    if (rv2b2 > EPS * EPS) {
+        vb3 = (+(f[2] * vnc + f[4] * bnc) * (f[2] * bnc + f[4] * mflux)
+               + (f[3] * vnc + f[5] * bnc) * (f[3] * bnc + f[5] * mflux)) / rv2b2;
+    }
+    const float bnvb = sgn * (bnca * (snc * vb2 - vnc * vb1) * (dirl * svci.x + dirr * svci.y)
+                              + bnsrv * (vb3 - vb2));
+    const float2 a6 = x2mul(mf, hn);
+    f[6] = a6.x + a6.y - bnvb;
 }
 
 }  // namespace mlau

@@ -532,7 +532,14 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
             const float dvtm = fminf(fminf(FI(SF_DVT, 1), FI(SF_DVT, 2)),
                                      fminf(FI(SF_DVU, 1), FI(SF_DVU, 2)));
             float F[7];
-            riemann_jumps(which, L, Rr, bn, gamma, dv0, dvtm, F, jp, jv);
+            if constexpr (ODR == 4 && WHICH == FLUX_MLAU) {
+                float2 P[7];
+#pragma unroll
+                for (int n = 0; n < 7; n++) P[n] = make_float2(L[n], Rr[n]);
+                flux_mlau_x2(P, bn, gamma, dv0, dvtm, F, jp, jv);
+            } else {
+                riemann_jumps(which, L, Rr, bn, gamma, dv0, dvtm, F, jp, jv);
+            }
             const float fct = 0.5f * (sl[7][tbl][tal] + sr[7][tb][ta]);
             const float fcu = 0.5f * (sl[8][tbl][tal] + sr[8][tb][ta]);
             F[4] -= fct;
