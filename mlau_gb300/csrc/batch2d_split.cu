@@ -6,6 +6,7 @@
 // FP32-split step (split3d.cu).
 #include "batch2d.cuh"
 #include "split_conv.cuh"
+#include "point_x2.cuh"
 
 namespace mlau {
 namespace {
@@ -118,6 +119,48 @@ __device__ void ph_rec(const BArgs &A, int nt, const BTile *tl, int D)
         if (D == 0) { src[1] = a.q[1]; src[2] = a.q[2]; src[3] = a.q[3]; src[4] = a.q[5]; src[5] = a.q[6]; }
         else { src[1] = a.q[2]; src[2] = a.q[3]; src[3] = a.q[1]; src[4] = a.q[6]; src[5] = a.q[4]; }
         const float2 *cn = D == 0 ? a.q[4] : a.q[5];
+        const int kb = D == 0 ? 4 : 5, kv = D == 0 ? 2 : 3;
+        const float *bface = a.bf[D];
+        const float mm = fmaxf(a.m2f[c - st], fmaxf(a.m2f[c], a.m2f[c + st]));
+        if (A.odr == 4 && mm < 1.f) {
+            // WCNS4 below Mach 1: packed FP32x2 form on the outer / inner
+            // point pairs of the perturbations (the centre one is zero)
+            float2 O[7], In[7];
+            float qc[7];
+            unsigned zero = 0;
+#pragma unroll
+            for (int n = 0; n < 7; n++) {
+                float2 h[5];
+#pragma unroll
+                for (int m = 0; m < 5; m++) h[m] = src[n][c + st * (m - 2)];
+                qc[n] = pf(h[2]);
+                const float2 t0 = x2sub(h[0], h[2]), t1 = x2sub(h[1], h[2]);
+                const float2 t3 = x2sub(h[3], h[2]), t4 = x2sub(h[4], h[2]);
+                O[n] = make_float2(t0.x + t0.y, t4.x + t4.y);
+                In[n] = make_float2(t1.x + t1.y, t3.x + t3.y);
+                bool z = true;
+#pragma unroll
+                for (int m = 0; m < 5; m++) z = z && h[m].x == 0.f && h[m].y == 0.f;
+                if (z) zero |= 1u << n;
+            }
+            float2 LR[7];
+            reconst_alfven_wcns4_x2(O, In, qc, pf(cn[c]), (float)I.gamma, LR);
+#pragma unroll
+            for (int n = 1; n <= 5; n++)
+                if (zero & (1u << n)) LR[n] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int n = 0; n < 7; n++) {
+                a.ulf[n][c + st] = LR[n].x;
+                a.urf[n][c] = LR[n].y;
+            }
+            const float a0 = qc[kb] * qc[1];
+            const float2 dao = x2fma(O[kb], x2add(x2k(qc[1]), O[1]), x2mul(x2k(qc[kb]), O[1]));
+            const float2 dai = x2fma(In[kb], x2add(x2k(qc[1]), In[1]), x2mul(x2k(qc[kb]), In[1]));
+            const float2 Av = lin4_pert_x2(dao, dai), V = lin4_pert_x2(O[kv], In[kv]);
+            a.ulf[7][c + st] = (a0 + Av.x) - bface[c + st] * (qc[kv] + V.x);
+            a.urf[7][c] = (a0 + Av.y) - bface[c] * (qc[kv] + V.y);
+            return;
+        }
         float dq[7][5], qc[7];
         unsigned zero = 0;
 #pragma unroll
@@ -135,7 +178,6 @@ __device__ void ph_rec(const BArgs &A, int nt, const BTile *tl, int D)
             if (z) zero |= 1u << n;
         }
         float ul[7], ur[7];
-        const float mm = fmaxf(a.m2f[c - st], fmaxf(a.m2f[c], a.m2f[c + st]));
         if (mm >= 1.f) reconst_full_core(A.odr, dq, qc, pf(cn[c]), (float)I.gamma, ul, ur);
         else reconst_alfven_core(A.odr, dq, qc, pf(cn[c]), (float)I.gamma, ul, ur);
 #pragma unroll
@@ -148,8 +190,6 @@ __device__ void ph_rec(const BArgs &A, int nt, const BTile *tl, int D)
         }
         // CT central part of the split tangential B flux:
         // X: By flux from (cy vx, vy); Y: Bx flux from (cx vy, vx)
-        const int kb = D == 0 ? 4 : 5, kv = D == 0 ? 2 : 3;
-        const float *bface = a.bf[D];
         const float a0 = qc[kb] * qc[1];
         float da[5];
 #pragma unroll
@@ -188,8 +228,15 @@ __device__ void ph_flux(const BArgs &A, int nt, const BTile *tl, int D)
         const float bn = a.bf[D][c];
         const float *dvt = a.dvf[D == 0 ? 1 : 0];
         float F[7];
-        riemann_jumps(I.flux, L, R, bn, (float)I.gamma, pd(src[1][c], src[1][c - st]),
-                      fminf(dvt[c - st], dvt[c]), F, jp, jmp[1]);
+        const float dv0 = pd(src[1][c], src[1][c - st]), dv1 = fminf(dvt[c - st], dvt[c]);
+        if (I.flux == FLUX_MLAU) {
+            float2 P[7];
+#pragma unroll
+            for (int n = 0; n < 7; n++) P[n] = make_float2(L[n], R[n]);
+            flux_mlau_x2(P, bn, (float)I.gamma, dv0, dv1, F, jp, jmp[1]);
+        } else {
+            riemann_jumps(I.flux, L, R, bn, (float)I.gamma, dv0, dv1, F, jp, jmp[1]);
+        }
         const float fc = 0.5f * (a.ulf[7][c] + a.urf[7][c]);
         F[4 + D] -= fc;
 #pragma unroll
