@@ -266,10 +266,13 @@ def run_e2e(args, R, st, meta, dt, M, prec):
     M.mhd_fd_ct_3d(*args_c, dt, meta["dx"], meta["dy"], meta["dz"], nx, ny, nz, 4, 4, 4,
                    meta["gamma"])  # warm-up: builds the cached device context
     R.barrier()
+    calls = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        tc = time.perf_counter()
         M.mhd_fd_ct_3d(*args_c, dt, meta["dx"], meta["dy"], meta["dz"], nx, ny, nz, 4, 4, 4,
                        meta["gamma"])
+        calls.append(time.perf_counter() - tc)
     t1 = time.perf_counter()
     R.barrier()
     el = R.max(t1 - t0)
@@ -284,7 +287,11 @@ def run_e2e(args, R, st, meta, dt, M, prec):
     return {"value": n ** 3 * args.steps * R.world / el, "unit": UNIT,
             "h2d_bytes_per_step": bytes_per_step, "d2h_bytes_per_step": bytes_per_step,
             "path": "C ABI mhd_fd_ct_3d (reference signature), pinned host arrays",
-            "placement": place}
+            "placement": place,
+            # per-call spread: the host link is shared with the machine's other
+            # GPUs, and its throughput moves between runs
+            "call_ms": {"min": 1e3 * min(calls), "median": 1e3 * float(np.median(calls)),
+                        "max": 1e3 * max(calls)}}
 
 
 def cpu_baseline(threads=None, n=96, steps=1):

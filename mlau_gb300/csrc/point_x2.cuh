@@ -14,7 +14,8 @@
 // Same formulas as wcns4_lr and reconst_alfven_core in point.cuh
 // (include/interp.h:186-238, include/mhd_eigen.h:609-684) up to FP32
 // rounding, with two rescalings that cancel in the normalised weights: the
-// smoothness indicators carry a factor 4 and the candidate stencils the 1/8.
+// smoothness indicators carry a factor 4 (and the weight epsilon 16) and the
+// candidate stencils the 1/8.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -40,7 +41,9 @@ __device__ __forceinline__ float2 x2fma(float2 a, float2 b, float2 c) { return _
 // lanes at the end.
 __device__ __forceinline__ float2 wcns4_pert_x2(float2 o, float2 i)
 {
-    const float eps = 1e-30f;
+    // the indicators below are 4 x the reference's, so their squares are 16 x:
+    // the epsilon is scaled with them (16 x the FP32 epsilon of wcns4_lr)
+    const float eps = 16e-30f;
     // 4 x the smoothness indicators of the outer stencils: (s0, s2)
     const float2 p = x2fma(x2k(-4.f), i, o);
     const float2 q = x2fma(x2k(-2.f), i, o);

@@ -66,14 +66,17 @@ def test_tile_shape_and_graph_do_not_change_results():
                 assert np.array_equal(o[k][v], outs[0][k][v])
 
 
-def test_split_vs_fp64_plain():
+@pytest.mark.parametrize("flux", ("lhlld", "mlau"))
+def test_split_vs_fp64_plain(flux):
+    """Below Mach 1 the split engine's WCNS4 runs in its packed FP32x2 form;
+    MLAU instances also take the packed MLAU flux."""
     st, m = ics.turbulence_2d(n=64, seed=2, vrms=0.5)
     dt = 0.4 * m["dx"] / m["vfast"]
-    with M.Sim(2, st["ro"].shape, dx=m["dx"], dy=m["dy"], odr=4, flux="lhlld") as s:
+    with M.Sim(2, st["ro"].shape, dx=m["dx"], dy=m["dy"], odr=4, flux=flux) as s:
         s.upload(st)
         s.step(dt, 40)
         ref = s.download()
-    with M.Batch([st["ro"].shape], [m["dx"]], [m["dy"]], [m["gamma"]], ["lhlld"], [0.4],
+    with M.Batch([st["ro"].shape], [m["dx"]], [m["dy"]], [m["gamma"]], [flux], [0.4],
                  [1.0]) as b:
         b.upload(0, st)
         b.set_fixed_dt(0, dt)
@@ -318,3 +321,26 @@ def test_batch1d_bad_state_retires():
         assert left == 0
         assert b.failed(cases[0]["slot"]) and not b.failed(cases[1]["slot"])
         assert b.info(cases[0]["slot"])[1] == 1
+
+
+def test_split_runs_a_marginal_request_to_its_end_like_fp64():
+    """Request 13 of the serving stream (509 x 675, LHLLD, Mach 0.81, beta
+    0.31) reaches its end time in FP64 while strong transients come close to
+    negative pressure.  The packed WCNS4 form must keep the reference's weight
+    epsilon (scaled with its rescaled smoothness indicators): with it 16 x
+    too small, this request retired on negative pressure at step 1262."""
+    from mlau_gb300 import serve
+    reqs = serve.make_requests(24, rate=5.0, seed=11)
+    r = next(q for q in reqs if q.rid == 13)
+    m = r.meta
+    assert r.kind == "2d" and m["flux"] == "lhlld"
+    steps = {}
+    for prec in (M.FP32_SPLIT, M.FP64):
+        with M.Batch.open(r.state["ro"].size, 1, precision=prec) as b:
+            s = b.add(r.state, m["dx"], m["dy"], m["gamma"], m["flux"], m["cfl"], m["t_end"])
+            while b.info(s)[2]:
+                b.run(512)
+            t, steps[prec], _ = b.info(s)
+            assert not b.failed(s), prec
+            assert t == pytest.approx(m["t_end"], rel=1e-12)
+    assert abs(steps[M.FP32_SPLIT] - steps[M.FP64]) <= 2

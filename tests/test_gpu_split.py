@@ -28,12 +28,15 @@ def run(st, m, steps, dt, precision, flux="mlau", odr=4):
         return s.download()
 
 
+@pytest.mark.parametrize("flux", ("mlau", "lhlld"))
 @pytest.mark.parametrize("mach", (1e-2, 1e-4))
-def test_split_density_l1_vs_fp64(mach):
+def test_split_density_l1_vs_fp64(mach, flux):
+    """WCNS4 with MLAU or LHLLD: the sweep instances specialised for these
+    schemes (packed FP32x2 reconstruction; MLAU also its packed flux)."""
     st, m = ics.turbulence_3d(n=32, mach=mach, seed=5)
     dt = 0.4 * m["dx"] / m["vfast"]
-    ref = run(st, m, 50, dt, M.FP64)
-    got = run(st, m, 50, dt, M.FP32_SPLIT)
+    ref = run(st, m, 50, dt, M.FP64, flux)
+    got = run(st, m, 50, dt, M.FP32_SPLIT, flux)
     err = {k: l1_rel(got[k], ref[k]) for k in ("ro", "en", "bx", "by", "bz")}
     assert err["ro"] <= RHO_L1_TOL, err
     assert err["en"] <= 1e-6 and max(err["bx"], err["by"], err["bz"]) <= 1e-5, err
