@@ -126,11 +126,12 @@ inline float2 host_ff(double x)
 
 // --- primitives (float-float recovery, FP32-pair output) -----------------
 // Face-to-centre B as the scheme's calc_bc, in float-float.
-__device__ __forceinline__ ff face2cen_ff(int odr, const double *b, long long w, long long st)
+// b: the faces w - st, w, w + st, w + 2 st.
+__device__ __forceinline__ ff face2cen_ff(int odr, const double b[4])
 {
-    const ff f1 = ff_from(b[w]), f2 = ff_from(b[w + st]);
+    const ff f1 = ff_from(b[1]), f2 = ff_from(b[2]);
     if (lin_odr(odr) <= 2) return ff_scale(ff_add(f1, f2), 0.5f);
-    const ff f0 = ff_from(b[w - st]), f3 = ff_from(b[w + 2 * st]);
+    const ff f0 = ff_from(b[0]), f3 = ff_from(b[3]);
     return ff_scale(ff_sub(ff_mul_f(ff_add(f1, f2), 9.0f), ff_add(f0, f3)), 0.0625f);
 }
 
@@ -141,23 +142,32 @@ ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, 
     if (!plane_cell(d, i, j, k)) return;
     const long long sy = d.nx, sz = (long long)d.nx * d.ny;
     const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
-    const ff cx = face2cen_ff(odr, f.s[5], w, 1);
-    const ff cy = face2cen_ff(odr, f.s[6], w, sy);
-    const ff cz = face2cen_ff(odr, f.s[7], w, sz);
     const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
-    const double ro = f.s[0][s];
+    // loads first, so that they are in flight together (the kernel waits on
+    // memory otherwise); the face stencils are at the cell's boundary source w
+    double bs[3][4], u[8];
+    const long long st[3] = {1, sy, sz};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int m = 0; m < 4; m++) bs[a][m] = f.s[5 + a][w + (m - 1) * st[a]];
+#pragma unroll
+    for (int v = 0; v < 8; v++) u[v] = f.s[v][s];
+    const ff cx = face2cen_ff(odr, bs[0]);
+    const ff cy = face2cen_ff(odr, bs[1]);
+    const ff cz = face2cen_ff(odr, bs[2]);
+    const double ro = u[0];
     // Velocities and the kinetic energy in FP32: rho v^2/2 enters the pressure
     // as an additive term, so its FP32 rounding (1e-7 of itself) stays below
     // the pressure's own FP32 resolution at any Mach number; the cancelling
     // terms E and B^2/2 are carried in float-float (48 bits).
     const float2 ro2 = split2(ro);
     const float rof = ro2.x + ro2.y, irof = 1.0f / rof;
-    const float vx = to_f32(f.s[1][s]) * irof, vy = to_f32(f.s[2][s]) * irof,
-                vz = to_f32(f.s[3][s]) * irof;
+    const float vx = to_f32(u[1]) * irof, vy = to_f32(u[2]) * irof, vz = to_f32(u[3]) * irof;
     const float v2 = vx * vx + vy * vy + vz * vz;
     const ff b2 = ff_add(ff_add(ff_sqr(cx), ff_sqr(cy)), ff_sqr(cz));
     const ff pr = ff_mul({gm1.x, gm1.y},
-                         ff_sub(ff_from(f.s[4][s]), ff_scale(ff_add_f(b2, rof * v2), 0.5f)));
+                         ff_sub(ff_from(u[4]), ff_scale(ff_add_f(b2, rof * v2), 0.5f)));
     const float2 pr2 = ff_pair(pr);
     g.q[0][sp] = ro2;
     g.q[1][sp] = make_float2(vx, 0.f);
@@ -167,14 +177,14 @@ ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, 
     g.q[5][sp] = ff_pair(cy);
     g.q[6][sp] = ff_pair(cz);
     g.q[7][sp] = pr2;
-    g.bf[0][sp] = to_f32(f.s[5][s]);
-    g.bf[1][sp] = to_f32(f.s[6][s]);
-    g.bf[2][sp] = to_f32(f.s[7][s]);
+    g.bf[0][sp] = to_f32(u[5]);
+    g.bf[1][sp] = to_f32(u[6]);
+    g.bf[2][sp] = to_f32(u[7]);
     // the first stage keeps U^n for the later stages' RK combine (this
     // kernel has loaded every state value of the cell already)
     if (save_u0)
 #pragma unroll
-        for (int v = 0; v < 8; v++) f.u0[v][s] = f.s[v][s];
+        for (int v = 0; v < 8; v++) f.u0[v][s] = u[v];
     g.m2[sp] = v2 / (gamma_f * (pr2.x + pr2.y) * irof);
 }
 
