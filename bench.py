@@ -291,7 +291,7 @@ def run_e2e(args, R, st, meta, dt, M, prec):
             # per-call spread: the host link is shared with the machine's other
             # GPUs, and its throughput moves between runs
             "call_ms": {"min": 1e3 * min(calls), "median": 1e3 * float(np.median(calls)),
-                        "max": 1e3 * max(calls)}}
+                        "max": 1e3 * max(calls), "each": [round(1e3 * c, 1) for c in calls]}}
 
 
 def cpu_baseline(threads=None, n=96, steps=1):
