@@ -596,6 +596,8 @@ void report(const char *who)
 
 int run_dropin(mlau_sim *c, double *const *h, double dt)
 {
+    // FP32-split: the host link's copies overlap the step where the data allow
+    if (c->sp) return split3d_step_host(c, dt, h);
     int rc = mlau_sim_upload(c, (const double *const *)h);
     if (rc == MLAU_OK) rc = mlau_sim_step(c, dt, 1);
     if (rc == MLAU_OK) rc = mlau_sim_download(c, h);

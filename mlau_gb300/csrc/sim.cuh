@@ -68,6 +68,8 @@ int plain1d_alloc(Sim *s);
 int plain1d_step(Sim *s, double dt);
 int split3d_alloc(Sim *s);
 int split3d_step(Sim *s, double dt);
+// one step of a state in host arrays (in place), copies overlapped with the step
+int split3d_step_host(Sim *s, double dt, double *const *h);
 void split3d_free(Sim *s);
 int split3d_check(Sim *s);
 int diff2d_resistive(Sim *s, double eta0, double dt);

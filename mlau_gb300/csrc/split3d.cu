@@ -85,6 +85,9 @@ struct SplitFields {
     int nblocks[3] = {};    // persistent grid per sweep
     int spec = 0;           // sweep instance: 0 run-time scheme, 1 WCNS4 + MLAU, 2 WCNS4 + LHLLD
     int *d_err = nullptr;   // set when a bounded wait gave up
+    // host-array steps (split3d_step_host): copy stream and slab events
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev_in[8] = {}, ev_out[8] = {};
 };
 
 namespace {
@@ -107,13 +110,14 @@ struct Dims {
 // Cell of this thread for the whole-grid kernels: one thread per cell of an
 // x-y plane (flattened, so no block runs mostly past the row end), one grid
 // row of blocks per z-plane.
-__device__ __forceinline__ bool plane_cell(const Dims &d, int &i, int &j, int &k)
+// row of blocks per z-plane, from plane k0.
+__device__ __forceinline__ bool plane_cell(const Dims &d, int &i, int &j, int &k, int k0 = 0)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.nx * d.ny) return false;
     j = t / d.nx;
     i = t - j * d.nx;
-    k = blockIdx.y;
+    k = k0 + blockIdx.y;
     return true;
 }
 
@@ -136,10 +140,10 @@ __device__ __forceinline__ ff face2cen_ff(int odr, const double b[4])
 }
 
 __global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, int save_u0)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, int save_u0, int k0)
 {
     int i, j, k;
-    if (!plane_cell(d, i, j, k)) return;
+    if (!plane_cell(d, i, j, k, k0)) return;
     const long long sy = d.nx, sz = (long long)d.nx * d.ny;
     const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
     const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
@@ -646,10 +650,10 @@ __device__ __forceinline__ void ld4(float v[4], const float *f, long long s, lon
 
 __global__ void __launch_bounds__(128)
 ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, float dtdx, float dtdy,
-          float dtdz, float2 ddx2, float2 ddy2, float2 ddz2)
+          float dtdz, float2 ddx2, float2 ddy2, float2 ddz2, int k0)
 {
     const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = d.oy + blockIdx.y, k = d.oz + blockIdx.z;
+    const int j = d.oy + blockIdx.y, k = k0 + blockIdx.z;
     if (i >= d.nx - d.ox) return;
     const long long sy = d.px, sz = d.px * d.ny;  // scratch strides
     const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
@@ -890,7 +894,16 @@ int split3d_alloc(Sim *s)
 
 void split3d_free(Sim *s)
 {
-    delete s->sp;
+    SplitFields *sf = s->sp;
+    if (sf && sf->cs) {
+        cudaStreamSynchronize(sf->cs);
+        for (int c = 0; c < 8; c++) {
+            cudaEventDestroy(sf->ev_in[c]);
+            cudaEventDestroy(sf->ev_out[c]);
+        }
+        cudaStreamDestroy(sf->cs);
+    }
+    delete sf;
     s->sp = nullptr;
 }
 
@@ -908,50 +921,158 @@ int split3d_check(Sim *s)
     return MLAU_OK;
 }
 
-int split3d_step(Sim *s, double dt)
-{
-    const Geometry &G = s->g;
-    PlainFields &f = s->f;
-    SplitFields &sf = *s->sp;
-    SplitPtrs &g = sf.p;
-    cudaStream_t st = s->stream;
-    const Dims d{G.nx, G.ny, G.nz, G.ox, G.oy, G.oz, sf.px};
-    const dim3 cb(128), cg(blocks_for((long long)G.nx * G.ny, 128), G.nz);
-    const dim3 ug(blocks_for(G.nx - 2 * G.ox, 128), G.ny - 2 * G.oy, G.nz - 2 * G.oz);
-    const float gam = (float)s->gamma;
-    for (int rk = 0; rk < s->nrk; rk++) {
+namespace {
+
+struct StepCtx {
+    Sim *s;
+    const Dims d;
+    const dim3 cb, cg, ug;
+    explicit StepCtx(Sim *sim)
+        : s(sim), d{sim->g.nx, sim->g.ny, sim->g.nz, sim->g.ox, sim->g.oy, sim->g.oz, sim->sp->px},
+          cb(128), cg(blocks_for((long long)sim->g.nx * sim->g.ny, 128), sim->g.nz),
+          ug(blocks_for(sim->g.nx - 2 * sim->g.ox, 128), sim->g.ny - 2 * sim->g.oy,
+             sim->g.nz - 2 * sim->g.oz)
+    {
+    }
+    // primitive recovery of planes [k0, k0 + nk)
+    void prim(int rk, int k0, int nk) const
+    {
+        ks_prim<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->f, s->sp->p, d, s->odr,
+                                                      host_ff(s->gamma - 1), (float)s->gamma,
+                                                      rk == 0, k0);
+    }
+    void aux() const { ks_aux<<<cg, cb, 0, s->stream>>>(s->sp->p, d); }
+    void sweeps() const
+    {
+        const float gam = (float)s->gamma;
+        launch_sweep<0>(s, *s->sp, d, gam);
+        launch_sweep<1>(s, *s->sp, d, gam);
+        launch_sweep<2>(s, *s->sp, d, gam);
+    }
+    void emf() const { ks_emf<<<cg, cb, 0, s->stream>>>(s->sp->p, d, s->odr); }
+    // RK combine + CT curl of the interior planes [k0, k0 + nk)
+    void update(int rk, double dt, int k0, int nk) const
+    {
+        const Geometry &G = s->g;
         const double t[3][2] = {{0.0, 1.0},
                                 {0.5 + (s->nrk - 2) * 0.25, 0.5 - (s->nrk - 2) * 0.25},
                                 {1. / 3., 2. / 3.}};
         const double ra = t[rk][0], rb = t[rk][1];
+        const double c24 = lin_odr(s->odr) > 2 ? 1.0 / 24.0 : 1.0;
+        const RkFF c{host_ff(ra), host_ff(rb), ra == 0.0 && rb == 1.0};
+        ks_update<<<dim3(ug.x, ug.y, nk), cb, 0, s->stream>>>(
+            s->f, s->sp->p, d, s->odr, c, (float)(dt / G.dx), (float)(dt / G.dy),
+            (float)(dt / G.dz), host_ff(dt / G.dx * c24), host_ff(dt / G.dy * c24),
+            host_ff(dt / G.dz * c24), k0);
+    }
+};
+
+}  // namespace
+
+int split3d_step(Sim *s, double dt)
+{
+    const Geometry &G = s->g;
+    const StepCtx x(s);
+    for (int rk = 0; rk < s->nrk; rk++) {
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
-            ks_prim<<<cg, cb, 0, st>>>(f, g, d, s->odr, host_ff(s->gamma - 1), (float)s->gamma,
-                                       rk == 0);
-            ks_aux<<<cg, cb, 0, st>>>(g, d);
+            x.prim(rk, 0, G.nz);
+            x.aux();
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_SWEEP);
-            launch_sweep<0>(s, sf, d, gam);
-            launch_sweep<1>(s, sf, d, gam);
-            launch_sweep<2>(s, sf, d, gam);
+            x.sweeps();
         }
         {
             TimedLaunch tl(&s->timer, KK_EMF);
-            ks_emf<<<cg, cb, 0, st>>>(g, d, s->odr);
+            x.emf();
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_UPDATE);
-            const double c24 = lin_odr(s->odr) > 2 ? 1.0 / 24.0 : 1.0;
-            const RkFF rk{host_ff(ra), host_ff(rb), ra == 0.0 && rb == 1.0};
-            ks_update<<<ug, cb, 0, st>>>(f, g, d, s->odr, rk, (float)(dt / G.dx),
-                                         (float)(dt / G.dy), (float)(dt / G.dz),
-                                         host_ff(dt / G.dx * c24), host_ff(dt / G.dy * c24),
-                                         host_ff(dt / G.dz * c24));
+            x.update(rk, dt, G.oz, G.nz - 2 * G.oz);
         }
         MLAU_CUDA(cudaGetLastError());
     }
     return MLAU_OK;
+}
+
+// One step of a state held in host arrays h[0..7] (the C-ABI drivers), in
+// place: the same kernels and arithmetic as upload + split3d_step + download,
+// with the host link's copies overlapped where the data allow.  The upload
+// goes in z-slabs on a copy stream, and the first stage's primitive recovery
+// of each slab starts once the slab above it is in (it reads face B up to two
+// planes up; the slabs holding ghost planes read their periodic sources at
+// the far end and wait for the whole state).  The last stage's update runs
+// slab by slab, and each slab's interior planes go back to the host while the
+// next slab updates; the ghost planes, which receive the periodic images
+// written by the update of the far end, go last.
+int split3d_step_host(Sim *s, double dt, double *const *h)
+{
+    const Geometry &G = s->g;
+    SplitFields &sf = *s->sp;
+    if (!sf.cs) {
+        MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cs, cudaStreamNonBlocking));
+        for (int c = 0; c < 8; c++) {
+            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_in[c], cudaEventDisableTiming));
+            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_out[c], cudaEventDisableTiming));
+        }
+    }
+    const int nz = G.nz, oz = G.oz, Nz = nz - 2 * oz;
+    const long long plane = (long long)G.nx * G.ny;
+    const int ns = std::max(1, std::min(8, Nz / 8));  // slabs of >= 8 interior planes
+    int b[9];  // slab c: planes [b[c], b[c + 1]); ghost planes with the end slabs
+    b[0] = 0;
+    for (int c = 1; c < ns; c++) b[c] = oz + (int)((long long)Nz * c / ns);
+    b[ns] = nz;
+    auto copy = [&](int k0, int k1, bool in) -> int {
+        for (int v = 0; v < 8; v++) {
+            double *dv = s->f.s[v] + k0 * plane, *hv = h[v] + k0 * plane;
+            const size_t bytes = sizeof(double) * (size_t)(k1 - k0) * plane;
+            MLAU_CUDA(in ? cudaMemcpyAsync(dv, hv, bytes, cudaMemcpyHostToDevice, sf.cs)
+                         : cudaMemcpyAsync(hv, dv, bytes, cudaMemcpyDeviceToHost, sf.cs));
+        }
+        return MLAU_OK;
+    };
+    // the previous use of the state on the compute stream ends before the upload
+    MLAU_CUDA(cudaEventRecord(sf.ev_out[0], s->stream));
+    MLAU_CUDA(cudaStreamWaitEvent(sf.cs, sf.ev_out[0], 0));
+    for (int c = 0; c < ns; c++) {
+        if (int rc = copy(b[c], b[c + 1], true)) return rc;
+        MLAU_CUDA(cudaEventRecord(sf.ev_in[c], sf.cs));
+    }
+    const StepCtx x(s);
+    for (int rk = 0; rk < s->nrk; rk++) {
+        if (rk == 0) {
+            for (int c = 1; c + 1 < ns; c++) {
+                MLAU_CUDA(cudaStreamWaitEvent(s->stream, sf.ev_in[c + 1], 0));
+                x.prim(0, b[c], b[c + 1] - b[c]);
+            }
+            MLAU_CUDA(cudaStreamWaitEvent(s->stream, sf.ev_in[ns - 1], 0));
+            x.prim(0, b[0], b[1] - b[0]);
+            if (ns > 1) x.prim(0, b[ns - 1], b[ns] - b[ns - 1]);
+        } else {
+            x.prim(rk, 0, nz);
+        }
+        x.aux();
+        x.sweeps();
+        x.emf();
+        if (rk + 1 < s->nrk) {
+            x.update(rk, dt, oz, Nz);
+        } else {
+            for (int c = 0; c < ns; c++) {
+                const int k0 = std::max(b[c], oz), k1 = std::min(b[c + 1], nz - oz);
+                x.update(rk, dt, k0, k1 - k0);
+                MLAU_CUDA(cudaEventRecord(sf.ev_out[c], s->stream));
+                MLAU_CUDA(cudaStreamWaitEvent(sf.cs, sf.ev_out[c], 0));
+                if (int rc = copy(k0, k1, false)) return rc;
+            }
+            if (int rc = copy(0, oz, false)) return rc;
+            if (int rc = copy(nz - oz, nz, false)) return rc;
+        }
+        MLAU_CUDA(cudaGetLastError());
+    }
+    MLAU_CUDA(cudaStreamSynchronize(sf.cs));
+    return split3d_check(s);
 }
 
 }  // namespace mlau

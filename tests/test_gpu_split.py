@@ -90,15 +90,21 @@ def test_split_ghosts_are_periodic_images():
         assert np.array_equal(np.pad(inner, 4, mode="wrap"), a), k
 
 
-def test_split_dropin_driver():
-    st, m = ics.turbulence_3d(n=16, mach=1e-2, seed=4)
+@pytest.mark.parametrize("shape", [(12, 16, 16), (16, 16, 16), (24, 16, 40), (32, 32, 32), (72, 24, 20)])
+def test_split_dropin_driver(shape):
+    """mhd_fd_ct_3d in FP32-split mode overlaps its host copies with the step
+    (z-slabs: 1, 2, 3, 4 and 8 of them here, ghost planes last); two calls in a
+    row equal two handle-API steps bit for bit."""
+    nzi, nyi, nxi = shape
+    st, m = ics.turbulence_3d(n=nxi, ny=nyi, nz=nzi, mach=1e-2, seed=4)
     nz, ny, nx = st["ro"].shape
-    ref = run(st, m, 1, 1e-3, M.FP32_SPLIT)
+    ref = run(st, m, 2, 1e-3, M.FP32_SPLIT)
     M.set_scheme(3, 4, "mlau", 3)
     M.set_precision(3, M.FP32_SPLIT)
     try:
-        M.mhd_fd_ct_3d(*[st[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")], 1e-3,
-                       m["dx"], m["dy"], m["dz"], nx, ny, nz, 4, 4, 4, m["gamma"])
+        for _ in range(2):
+            M.mhd_fd_ct_3d(*[st[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
+                           1e-3, m["dx"], m["dy"], m["dz"], nx, ny, nz, 4, 4, 4, m["gamma"])
     finally:
         M.set_precision(3, M.FP64)
         M.release_dropin()
