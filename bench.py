@@ -196,12 +196,15 @@ def roofline(timing, n, off, peaks, precision):
 
 
 # --- our arm -----------------------------------------------------------------
-def run_ours(args, R: Ranks, precision, st, meta):
+PRECISIONS = {"fp64": "FP64", "split": "FP32_SPLIT", "split_f64": "FP32_SPLIT_F64"}
+
+
+def run_ours(args, R: Ranks, precision, st, meta, e2e=True):
     import mlau_gb300 as M
 
     M.set_device(R.local)
     n, off = args.n, 4
-    prec = M.FP32_SPLIT if precision == "split" else M.FP64
+    prec = getattr(M, PRECISIONS[precision])
     sim = M.Sim(3, st["ro"].shape, off=off, dx=meta["dx"], dy=meta["dy"], dz=meta["dz"],
                 gamma=meta["gamma"], odr=4, flux="mlau", nrk=3, precision=prec)
     sim.upload(st)
@@ -227,10 +230,35 @@ def run_ours(args, R: Ranks, precision, st, meta):
               "clocks": clk.summary(), "dt": dt, "launches": launches, "peaks": peaks,
               "device_bytes": sim.device_bytes}
     # end to end through the C ABI drop-in driver with pinned host buffers
-    result["e2e"] = run_e2e(args, R, st, meta, dt, M, prec)
-    result["final"] = sim.download()
+    if e2e:
+        result["e2e"] = run_e2e(args, R, st, meta, dt, M, prec)
     sim.close()
     return result
+
+
+def run_accuracy(n, mach, steps, seed=8):
+    """The 3D configuration's accuracy record: `steps` RK3 steps at a fixed dt
+    (CFL 0.4 of the initial state) from one seeded state, in plain FP64 and in
+    both FP32-split forms; per-variable relative L1 of each split result
+    against the FP64 one, and max |div B| * dx / max |B| of every result."""
+    import mlau_gb300 as M
+    from mlau_gb300 import ics
+    st, m = ics.turbulence_3d(n=n, mach=mach, seed=seed)
+    dt = 0.4 * m["dx"] / m["vfast"]
+    out, ms = {}, {}
+    for name in ("fp64", "split", "split_f64"):
+        with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"], gamma=m["gamma"],
+                   odr=4, flux="mlau", nrk=3, precision=getattr(M, PRECISIONS[name])) as s:
+            s.upload(st)
+            ms[name] = s.time_steps(dt, steps)
+            out[name] = s.download()
+    rec = {"grid": [n, n, n], "rms_mach": mach, "steps": steps, "dt": dt, "seed": seed,
+           "tolerance_ro": 1e-6,
+           "div_b": {k: ics.div_b_3d(v, m["dx"], m["dy"], m["dz"]) for k, v in out.items()},
+           "ms_per_step": {k: v / steps for k, v in ms.items()}}
+    for name in ("split", "split_f64"):
+        rec[f"l1_{name}_vs_fp64"] = rel_l1(out[name], out["fp64"])
+    return rec
 
 
 def rel_l1(a, b, off=4):
@@ -294,14 +322,14 @@ def run_e2e(args, R, st, meta, dt, M, prec):
                         "max": 1e3 * max(calls), "each": [round(1e3 * c, 1) for c in calls]}}
 
 
-def cpu_baseline(threads=None, n=96, steps=1):
+def cpu_baseline(threads=None, n=256, steps=2, mach=1e-2):
     """The CPU restatement of the reference driver (oracle/, bit-identical to
     the reference and within ~20% of its speed) on this host's cores."""
     os.environ["OMP_NUM_THREADS"] = str(threads or os.cpu_count())
     from mlau_gb300 import ics
     from oracle import Port
 
-    st, meta = ics.turbulence_3d(n=n, mach=1e-2, seed=7)
+    st, meta = ics.turbulence_3d(n=n, mach=mach, seed=7)
     dt = 0.4 * meta["dx"] / meta["vfast"]
     Port.step3d(st, dt, meta["dx"], meta["dy"], meta["dz"], odr=4, flux="mlau")  # warm
     t0 = time.perf_counter()
@@ -316,8 +344,9 @@ def cpu_baseline(threads=None, n=96, steps=1):
 
 def run_reference(args, R: Ranks):
     """--impl reference: the reference's CPU implementation of the path (its C
-    restatement; the reference's own object files do not travel to this host)
-    with all host threads; each step is a bounded 128^3 sample of the workload."""
+    restatement, bit-identical to the reference; the reference's own object
+    files do not travel to this host) with all host threads, on the
+    benchmark's own workload (--ref-n defaults to --n)."""
     if R.rank != 0:
         return
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
@@ -339,7 +368,10 @@ def run_reference(args, R: Ranks):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded random-phase ICs)",
             "config": workload_desc(args.n, args.mach, "fp64-plain") | {
-                "sample": f"{n}^3 interior per step (bounded sample of the {args.n}^3 workload)"},
+                "sample": f"{n}^3 interior per step" + (
+                    " (the benchmark's own workload)" if n == args.n
+                    else f" (bounded sample of the {args.n}^3 workload)"),
+                "same_config": n == args.n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{n}^3 interior x {args.steps} steps"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -532,22 +564,25 @@ def batch2d_requests(n_inst, seed, n2d=(64, 1024), t_end=(0.05, 0.5)):
                                t_end_2d=t_end, split_frac=1.0)
 
 
-def run_batch2d(args):
+def run_batch2d(args, n_inst=None, steps=None, warmup=None):
     """Batched 2D engine, FP32-split: all instances in one persistent
     cooperative launch per step, tile shape from the autotuner, steps replayed
     from captured graphs; zone-updates/s over the instances still running."""
     import mlau_gb300 as M
-    reqs = batch2d_requests(args.batch_n, seed=5)
+    n_inst = n_inst or args.batch_n
+    steps = steps or args.steps
+    warmup = warmup or args.warmup
+    reqs = batch2d_requests(n_inst, seed=5)
     cells = sum(r.state["ro"].size for r in reqs)
     b = M.Batch.open(cells, len(reqs), precision=M.FP32_SPLIT, odr=4)
     slots = [b.add(r.state, r.meta["dx"], r.meta["dy"], r.meta["gamma"], r.meta["flux"],
                    r.meta["cfl"], r.meta["t_end"]) for r in reqs]
     tw, th, tune_ms = b.autotune(steps=2)
-    b.run(args.warmup, steps_per_graph=args.warmup)
+    b.run(warmup, steps_per_graph=warmup)
     before = [b.info(s)[1] for s in slots]
     active = sum(b.info(s)[2] for s in slots)
     with ClockSampler(0) as clk:
-        left, ms = b.run(args.steps, steps_per_graph=args.steps)
+        left, ms = b.run(steps, steps_per_graph=steps)
     # zone-updates actually done: instances that retire mid-run stop counting
     zones = sum(r.interior * (b.info(s)[1] - n0) for r, s, n0 in zip(reqs, slots, before))
     failed = sum(b.failed(s) for s in slots)
@@ -555,8 +590,8 @@ def run_batch2d(args):
     b.close()
     return {"metric": "batched 2D zone-updates/s (uneven instances, one persistent launch per "
                       "step, FP32-split)",
-            "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "value": v, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
             "config": {"workload": f"{len(reqs)} periodic 2D instances, sizes log-uniform "
                                    f"64..1024 per axis, solver/gamma uniform, Mach U[1e-3,2], "
@@ -564,9 +599,9 @@ def run_batch2d(args):
                        "zone_updates": zones, "instances_active_at_start": active,
                        "instances_active_at_end": left,
                        "tile": [tw, th], "autotune_ms": tune_ms,
-                       "graph_steps": args.steps, "failed_instances": failed,
+                       "graph_steps": steps, "failed_instances": failed,
                        "l2": "working set >> 129 MB L2"},
-            "gpu_launches": args.steps, "clocks": clk.summary()}
+            "gpu_launches": steps, "clocks": clk.summary()}
 
 
 def run_serve(args):
@@ -626,12 +661,20 @@ def main():
     ap.add_argument("--precision", choices=("both", "fp64", "split"), default="both",
                     help="both: FP32-split is the headline value, FP64 beside it")
     ap.add_argument("--workload", choices=("step3d", "step2d", "step1d", "batch2d", "serve",
-                                           "mrx2d"),
+                                           "mrx2d", "accuracy3d"),
                     default="step3d")
     ap.add_argument("--n2d", type=int, default=512)
     ap.add_argument("--cpu-steps", type=int, default=2)
-    ap.add_argument("--ref-n", type=int, default=128)
+    ap.add_argument("--ref-n", type=int, default=None,
+                    help="interior size of the reference arm's steps (default: --n, the "
+                         "benchmark's own workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the end-to-end drop-in measurement (profiling runs)")
+    ap.add_argument("--batch-sample", type=int, default=64,
+                    help="instances of the batched-engine sample in the default line (0: skip)")
+    ap.add_argument("--accuracy-steps", type=int, default=200,
+                    help="steps of the split-vs-FP64 accuracy record (0: skip it)")
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--serve-n", type=int, default=24)
     ap.add_argument("--rates", default="5,50,200")
@@ -642,6 +685,8 @@ def main():
     ap.add_argument("--serve-t-end-max", type=float, default=0.5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.ref_n is None:
+        args.ref_n = args.n
     R = Ranks()
     try:
         if args.impl == "reference":
@@ -656,6 +701,23 @@ def main():
             if R.rank == 0:
                 print(json.dumps(run_mrx2d(args)), flush=True)
             return
+        if args.workload == "accuracy3d":
+            if R.rank == 0:
+                recs = [run_accuracy(args.n, mach, args.accuracy_steps)
+                        for mach in sorted({args.mach, 1e-4}, reverse=True)]
+                zu = args.n ** 3 / 1e3
+                print(json.dumps({
+                    "metric": "3D split-vs-FP64 relative L1 after the configuration's steps",
+                    "value": max(r["l1_split_vs_fp64"]["ro"] for r in recs),
+                    "unit": "relative L1 of density", "higher_is_better": False, "n_gpus": 1,
+                    "steps": args.accuracy_steps, "dtype": "f32+f64 vs f64",
+                    "data": "synthetic (seeded random-phase ICs)",
+                    "config": workload_desc(args.n, args.mach, "fp64 and both FP32-split forms"),
+                    "zone_updates_per_s": {
+                        r["rms_mach"]: {k: zu / v for k, v in r["ms_per_step"].items()}
+                        for r in recs},
+                    "accuracy": recs}), flush=True)
+            return
         if args.workload == "batch2d":
             if R.rank == 0:
                 print(json.dumps(run_batch2d(args)), flush=True)
@@ -667,12 +729,15 @@ def main():
         from mlau_gb300 import ics
         st, meta = ics.turbulence_3d(n=args.n, mach=args.mach, seed=1000 + R.rank)
         precs = ("split", "fp64") if args.precision == "both" else (args.precision,)
-        res = {p: run_ours(args, R, p, st, meta) for p in precs}
+        res = {p: run_ours(args, R, p, st, meta, e2e=not args.no_e2e) for p in precs}
+        if args.precision == "both":
+            # the split form with FP64 state arithmetic, device-timed beside it
+            res["split_f64"] = run_ours(args, R, "split_f64", st, meta, e2e=False)
         if R.rank != 0:
             return
         head = precs[0]
         r = res[head]
-        prec_name = "fp64" if head == "fp64" else "fp32-split"
+        prec_name = {"fp64": "fp64", "split": "fp32-split", "split_f64": "fp32-split-f64"}[head]
         line = {
             "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": R.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
@@ -683,7 +748,7 @@ def main():
                 "parallelism": f"replicas x{R.world}" if R.world > 1 else "single GPU",
                 "dt": r["dt"]},
             "roofline": roofline(r["timing"], args.n, 4, r["peaks"], head),
-            "e2e": r["e2e"],
+            "e2e": r.get("e2e"),
             "gpu_launches": r["launches"],
             "clocks": r["clocks"],
             "kernel_ms": {k: {"launches": c, "total_ms": t} for k, (c, t) in r["timing"].items()},
@@ -694,16 +759,34 @@ def main():
         if "fp64" in res and head != "fp64":
             f = res["fp64"]
             line["fp64"] = {
-                "value": f["value"], "ms_per_step": f["ms_per_step"], "e2e": f["e2e"],
+                "value": f["value"], "ms_per_step": f["ms_per_step"], "e2e": f.get("e2e"),
                 "roofline": roofline(f["timing"], args.n, 4, f["peaks"], "fp64"),
                 "gpu_launches": f["launches"], "clocks": f["clocks"],
                 "kernel_ms": {k: {"launches": c, "total_ms": t}
                               for k, (c, t) in f["timing"].items()}}
             line["split_over_fp64"] = r["value"] / f["value"]
-            line["l1_vs_fp64"] = rel_l1(r["final"], f["final"]) | {
-                "after_steps": args.warmup + args.steps, "tolerance_ro": 1e-6}
+        if "split_f64" in res:
+            q = res["split_f64"]
+            line["split_f64"] = {
+                "what": "FP32 reconstruction / Riemann solver / EMFs, with pressure recovery, "
+                        "RK accumulation and CT curl in FP64 arithmetic (float-float in the "
+                        "headline form)",
+                "value": q["value"], "ms_per_step": q["ms_per_step"],
+                "over_fp64": q["value"] / res["fp64"]["value"] if "fp64" in res else None,
+                "gpu_launches": q["launches"],
+                "kernel_ms": {k: {"launches": c, "total_ms": t}
+                              for k, (c, t) in q["timing"].items()}}
+        if args.batch_sample > 0 and R.world == 1 and args.precision == "both":
+            # a bounded sample of the batched engine (uneven 2D instances)
+            bl = run_batch2d(args, n_inst=args.batch_sample, steps=5, warmup=3)
+            line["batch2d_sample"] = {k: bl[k] for k in ("metric", "value", "unit", "ms_per_step",
+                                                         "steps", "config", "clocks")}
+        if args.accuracy_steps > 0 and R.world == 1 and args.precision == "both":
+            # the configuration's 200-step accuracy record at both Mach numbers
+            line["accuracy"] = [run_accuracy(args.n, mach, args.accuracy_steps)
+                                for mach in sorted({args.mach, 1e-4}, reverse=True)]
         if not args.no_cpu_baseline and R.world == 1:
-            line["cpu_baseline"] = cpu_baseline()
+            line["cpu_baseline"] = cpu_baseline(n=args.n, mach=args.mach)
         print(json.dumps(line), flush=True)
     finally:
         R.close()

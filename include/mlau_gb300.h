@@ -43,8 +43,13 @@ enum {
 
 /* Riemann solvers of include/mhd_flux.h. */
 enum { MLAU_FLUX_MLAU = 0, MLAU_FLUX_LHLLD = 1, MLAU_FLUX_HLLD = 2, MLAU_FLUX_ROE = 3 };
-/* Arithmetic of the reconstruction and Riemann solver. */
-enum { MLAU_FP64 = 0, MLAU_FP32_SPLIT = 1 };
+/* Arithmetic of the step.  MLAU_FP64: the reference's, bit for bit.
+ * MLAU_FP32_SPLIT: reconstruction, Riemann solver, edge EMFs, CT weights and
+ * shock sensors in FP32; the conserved state stays FP64, and its RK
+ * accumulation, the pressure recovery and the CT curl run in float-float
+ * (hi + lo FP32 pairs, ~48 bits) on the FP32 pipe.  MLAU_FP32_SPLIT_F64: the
+ * same FP32 parts, with those three steps in FP64 arithmetic instead (3D). */
+enum { MLAU_FP64 = 0, MLAU_FP32_SPLIT = 1, MLAU_FP32_SPLIT_F64 = 2 };
 /* 1D boundaries. */
 enum { MLAU_BC1D_OPEN = 0, MLAU_BC1D_PERIODIC = 1 };
 /* Eigen-system of the characteristic projection where the largest sonic
@@ -142,7 +147,7 @@ int mlau_set_bc_1d(int bc);
  * tables give way to them at load time), else zeros. */
 int mlau_boundary_tables(int *dnx, int *dny, int *dnz);
 /* Arithmetic of the drop-in 3D driver: MLAU_FP64 (default; the reference's
- * arithmetic bit for bit) or MLAU_FP32_SPLIT. */
+ * arithmetic bit for bit), MLAU_FP32_SPLIT or MLAU_FP32_SPLIT_F64. */
 int mlau_set_precision(int dim, int precision);
 /* Free the device memory cached by the drop-in drivers (it is kept between
  * calls so that a time loop does not reallocate every step). */
@@ -156,9 +161,9 @@ void mlau_clear_error(void);
 typedef struct mlau_sim mlau_sim;
 
 /* dim 3: nx,ny,nz padded sizes; dim 2: nz = 1; dim 1: ny = nz = 1.
- * xoff/yoff/zoff: ghost depth (>= 3; the reference uses 4).  Interior width
+ * xoff/yoff/zoff: ghost depth (>= 4, as the reference fixes it).  Interior width
  * must be at least the ghost depth.  odr 1..6, flux MLAU_FLUX_*, nrk 1..3,
- * precision MLAU_FP64 or MLAU_FP32_SPLIT (3D only). */
+ * precision MLAU_FP64, or MLAU_FP32_SPLIT / MLAU_FP32_SPLIT_F64 (3D only). */
 int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, int yoff,
                     int zoff, double dx, double dy, double dz, double gamma, int odr, int flux,
                     int nrk, int precision);
@@ -344,7 +349,10 @@ int mlau_batch1d_add(mlau_batch *b, int nx, double dx, double bx, double gamma, 
  * stream) and the call returns without waiting.  All calls share the one
  * array: calls that overlap on the GPU (different streams, no ordering) race
  * on it.  Nothing in the scratch needs clearing between calls: every element
- * a step reads is written earlier in the same step. */
+ * a step reads is written earlier in the same step (ghost depth xoff >= 4, as
+ * the reference fixes it; smaller depths are rejected).  The resolved address
+ * is cached per device for the life of the process, so cudaDeviceReset is not
+ * supported once this entry point has run on that device. */
 #define MLAU_NOALLOC_1D_MAX_NX 16392
 int mlau_fd4c_1d_noalloc(double *ro, double *mx, double *my, double *mz, double *en, double *by,
                          double *bz, double bx, double dt, double dx, int nx, int xoff,

@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmlau_gb300.so")
 
 FLUX = {"mlau": 0, "lhlld": 1, "hlld": 2, "roe": 3}
 EIGEN = {"full": 0, "miyoshi": 1}
-FP64, FP32_SPLIT = 0, 1
+FP64, FP32_SPLIT, FP32_SPLIT_F64 = 0, 1, 2
 OUT_F64, OUT_F32_RANK = 0, 1
 BC1D = {"open": 0, "periodic": 1}
 VARS = ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")

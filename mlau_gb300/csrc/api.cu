@@ -86,18 +86,21 @@ KernelTimer::~KernelTimer()
 
 static int check_geometry(int dim, int nx, int ny, int nz, int ox, int oy, int oz)
 {
-    auto ok_axis = [](int n, int off) { return off >= 3 && n - 2 * off >= off; };
+    // ghost depth 4 as the reference fixes it (3D/MPI/OTvortex/global.hpp:36-37,
+    // 1D/SERIAL/shock/main.cpp:8): the flux kernels fill faces [3, n-2) and a
+    // 4th-order update from the first interior cell reads one face below it
+    auto ok_axis = [](int n, int off) { return off >= 4 && n - 2 * off >= off; };
     if (dim < 1 || dim > 3) { set_error("dim must be 1, 2 or 3 (got %d)", dim); return 0; }
     if (!ok_axis(nx, ox)) {
-        set_error("x: need ghost depth >= 3 and interior width >= ghost depth (nx=%d, off=%d)", nx, ox);
+        set_error("x: need ghost depth >= 4 and interior width >= ghost depth (nx=%d, off=%d)", nx, ox);
         return 0;
     }
     if (dim >= 2 && !ok_axis(ny, oy)) {
-        set_error("y: need ghost depth >= 3 and interior width >= ghost depth (ny=%d, off=%d)", ny, oy);
+        set_error("y: need ghost depth >= 4 and interior width >= ghost depth (ny=%d, off=%d)", ny, oy);
         return 0;
     }
     if (dim == 3 && !ok_axis(nz, oz)) {
-        set_error("z: need ghost depth >= 3 and interior width >= ghost depth (nz=%d, off=%d)", nz, oz);
+        set_error("z: need ghost depth >= 4 and interior width >= ghost depth (nz=%d, off=%d)", nz, oz);
         return 0;
     }
     if ((double)nx * ny * nz > 2.0e9) { set_error("grid too large for 32-bit cell indices"); return 0; }
@@ -107,7 +110,7 @@ static int check_geometry(int dim, int nx, int ny, int nz, int ox, int oy, int o
 int launches_per_step(const Sim *s)
 {
     // kernels per RK stage (device-to-device copies are not counted)
-    if (s->precision == MLAU_FP32_SPLIT) return s->nrk * 7;
+    if (s->sp) return s->nrk * 7;
     if (s->g.dim == 3) return s->nrk * (s->walls3d ? 12 : 10);
     if (s->g.dim == 2) return s->nrk * (s->walls2d ? 10 : 8);
     return s->nrk * 4 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
@@ -138,7 +141,7 @@ int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, i
         set_error("scheme out of range (odr 1..6, flux 0..3, nrk 1..3)");
         return MLAU_ERR_ARG;
     }
-    if (precision != MLAU_FP64 && !(precision == MLAU_FP32_SPLIT && dim == 3)) {
+    if (precision != MLAU_FP64 && !(is_split(precision) && dim == 3)) {
         set_error("precision %d not available for dim %d", precision, dim);
         return MLAU_ERR_ARG;
     }
@@ -161,7 +164,7 @@ int mlau_sim_create(mlau_sim **out, int dim, int nx, int ny, int nz, int xoff, i
     }
     s->timer.stream = s->stream;
     int rc;
-    if (precision == MLAU_FP32_SPLIT) rc = split3d_alloc(s);
+    if (is_split(precision)) rc = split3d_alloc(s);
     else if (dim == 3) rc = plain3d_alloc(s);
     else if (dim == 2) rc = plain2d_alloc(s);
     else rc = plain1d_alloc(s);
@@ -323,7 +326,7 @@ int mlau_sim_set_bc_1d(mlau_sim *s, int bc)
 
 static int step_once(mlau_sim *s, double dt)
 {
-    if (s->precision == MLAU_FP32_SPLIT) return split3d_step(s, dt);
+    if (s->sp) return split3d_step(s, dt);
     if (s->g.dim == 3) return plain3d_step(s, dt);
     if (s->g.dim == 2) return plain2d_step(s, dt);
     return plain1d_step(s, dt);
@@ -638,7 +641,7 @@ int mlau_set_precision(int dim, int precision)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     init_scheme();
-    if (dim < 1 || dim > 3 || (precision != MLAU_FP64 && !(precision == MLAU_FP32_SPLIT && dim == 3))) {
+    if (dim < 1 || dim > 3 || (precision != MLAU_FP64 && !(is_split(precision) && dim == 3))) {
         set_error("mlau_set_precision: precision %d not available for dim %d", precision, dim);
         return MLAU_ERR_ARG;
     }

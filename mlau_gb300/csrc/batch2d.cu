@@ -254,7 +254,7 @@ extern "C" {
 int mlau_batch_open(mlau_batch **out, int precision, long long capacity_cells, int max_inst,
                     int off, int odr)
 {
-    if (!out || capacity_cells <= 0 || max_inst <= 0 || off < 3 || odr < 1 || odr > 6 ||
+    if (!out || capacity_cells <= 0 || max_inst <= 0 || off < 4 || odr < 1 || odr > 6 ||
         (precision != MLAU_FP64 && precision != MLAU_FP32_SPLIT)) {
         set_error("batch: bad arguments");
         return MLAU_ERR_ARG;

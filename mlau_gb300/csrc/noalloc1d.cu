@@ -74,7 +74,7 @@ extern "C" int mlau_fd4c_1d_noalloc(double *ro, double *mx, double *my, double *
                   "(use the mlau_sim handle API for larger grids)", nx, kMaxNx);
         return MLAU_ERR_ARG;
     }
-    if (xoff < 3 || nx - 2 * xoff < xoff || odr < 1 || odr > 6 || flux < 0 || flux > 3 ||
+    if (xoff < 4 || nx - 2 * xoff < xoff || odr < 1 || odr > 6 || flux < 0 || flux > 3 ||
         nrk < 1 || nrk > 3 || (bc != MLAU_BC1D_OPEN && bc != MLAU_BC1D_PERIODIC) ||
         !(gamma > 1.0) || !(dx > 0)) {
         set_error("mlau_fd4c_1d_noalloc: bad geometry or scheme");

@@ -20,6 +20,12 @@
 #else
 #define MLAU_HD inline
 #include <cmath>
+#if defined(__GNUC__)
+// host compilers see the device loops' unroll hints
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Wunknown-pragmas"
+#define MLAU_POINT_DIAG_PUSHED
+#endif
 #endif
 
 namespace mlau {
@@ -146,6 +152,62 @@ template <class T> MLAU_HD void wcns4_lr(T f0, T f1, T f2, T f3, T f4, T &fl, T 
     w1 *= r;
     w2 = T(1.0) - w0 - w1;
     fr = T(0.125) * (+w2 * qa + w1 * qb + w0 * qc);
+}
+
+// One-sided face values of include/interp.h - the value between f0 and fd
+// (MUSCL, :25-28, :39-43, :55-60) or between f and fdn (WCNS, :75-104,
+// :148-184).  No driver calls them; they complete the header's interface.
+template <class T> MLAU_HD T muscl_mm_f(T fu, T f0, T fd)
+{
+    return f0 - T(0.5) * minmod(fu - f0, f0 - fd);
+}
+template <class T> MLAU_HD T muscl_mc_f(T fu, T f0, T fd)
+{
+    const T alpha = T(2.0);
+    return f0 - T(0.5) * minmod(alpha * minmod(fu - f0, f0 - fd), T(0.5) * (fu - fd));
+}
+template <class T> MLAU_HD T muscl_kr_f(T fu, T f0, T fd)
+{
+    const T d1 = T(2.0) * (fu - f0);
+    const T d2 = T(2.0) * (f0 - fd);
+    return f0 - T(0.5) * minmod3(d1, d2, (T(0.5) * d1 + d2) / T(3.0));
+}
+template <class T> MLAU_HD T wcns3_f(T fup, T f, T fdn)
+{
+    const T eps = wcns_eps<T>();
+    T d0 = fup - f, d1 = fdn - f;
+    T s0 = d0 * d0, s1 = d1 * d1;
+    T t = fup - T(2.0) * f + fdn;
+    t = t * t;
+    T a = T(0.25) * (T(1.0) + t / (s0 + eps));
+    T b = T(0.75) * (T(1.0) + t / (s1 + eps));
+    a /= (a + b);
+    b = T(1.0) - a;
+    return T(0.5) * (a * (-fup + T(3.0) * f) + b * (f + fdn));
+}
+template <class T> MLAU_HD T wcns4_f(T fuu, T fup, T f, T fdn, T fdd)
+{
+    const T eps = wcns_eps<T>();
+    T p, q, s0, s1, s2;
+    p = fuu - T(4.0) * fup + T(3.0) * f;
+    q = fuu - T(2.0) * fup + f;
+    s0 = T(13. / 12.) * q * q + T(0.25) * p * p;
+    p = fup - fdn;
+    q = fup - T(2.0) * f + fdn;
+    s1 = T(13. / 12.) * q * q + T(0.25) * p * p;
+    p = T(3.0) * f - T(4.0) * fdn + fdd;
+    q = f - T(2.0) * fdn + fdd;
+    s2 = T(13. / 12.) * q * q + T(0.25) * p * p;
+    T w0 = T(0.075) / (s0 * s0 + eps);
+    T w1 = T(0.650) / (s1 * s1 + eps);
+    T w2 = T(0.275) / (s2 * s2 + eps);
+    const T den = T(1.0) / (w0 + w1 + w2);
+    w0 *= den;
+    w1 *= den;
+    w2 = T(1.0) - w0 - w1;
+    return T(0.125) * (+w0 * (T(3.0) * fuu - T(10.0) * fup + T(15.0) * f)
+                       + w1 * (-fup + T(6.0) * f + T(3.0) * fdn)
+                       + w2 * (+T(3.0) * f + T(6.0) * fdn - fdd));
 }
 
 // calc_flr of the drivers (3D/MPI/OTvortex/mhd_fd_ct_3d.c:65-78).
@@ -424,21 +486,104 @@ MLAU_HD void reconst_full(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur
     zero_guard(q, ul, ur);
 }
 
-// Fast + Alfven projection of Miyoshi (mhd_m_reconst with mhd_eigen_mi,
-// mhd_eigen.h:194-324, 532-607; the slow mode is ignored), the header's
-// alternative to the full system.  The reference multiplies the dense 7x7
-// rows, zeros included, in index order; so does this (the zero products
-// decide signed zeros), with its rows written out.
-template <class T>
-MLAU_HD void reconst_miyoshi(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+// The eigen-systems as include/mhd_eigen.h returns them: eigenvalues al[7]
+// (the full system only; the others leave al untouched, as the reference's
+// do), left eigenvectors as rows L[n][k] and right eigenvectors as R[n][k]
+// (l_{n+1}[k] and r_{n+1}[k] in the header's 1-based names), every entry -
+// zeros and their signs included - set as the header sets it.  The sparse
+// projections above use the same coefficients without the zeros.
+template <class T> MLAU_HD void mirror_row(const T a[7], T b[7])
 {
-    const T ro = q[0][2], by = q[4][2], bz = q[5][2], pr = q[6][2];
+    b[0] = a[0]; b[1] = -a[1]; b[2] = -a[2]; b[3] = -a[3];
+    b[4] = a[4]; b[5] = a[5]; b[6] = a[6];
+}
+
+// mhd_eigen_st (mhd_eigen.h:24-192): fast, Alfven and slow pairs, entropy.
+template <class T>
+MLAU_HD void eigen_st_dense(T ro, T vx, T vy, T vz, T bx, T by, T bz, T pr, T gamma, T al[7],
+                            T L[7][7], T R[7][7])
+{
+    (void)vy;
+    (void)vz;
+    Eigen7<T> E;
+    eigen_full(ro, vx, bx, by, bz, pr, gamma, E);
+    const T z = T(0);
+#pragma unroll
+    for (int n = 0; n < 7; n++) al[n] = E.lam[n];
+    L[0][0] = z;
+    L[1][0] = z; L[1][1] = z; L[1][6] = z;
+    L[2][0] = z;
+#pragma unroll
+    for (int k = 1; k < 7; k++) { L[0][k] = E.a[k]; L[2][k] = E.c[k]; }
+#pragma unroll
+    for (int k = 2; k < 6; k++) L[1][k] = E.b[k];
+    L[3][0] = T(1.0);
+    L[3][1] = z; L[3][2] = z; L[3][3] = z; L[3][4] = z; L[3][5] = z;
+    L[3][6] = E.d6;
+    R[1][0] = z; R[1][1] = z; R[1][6] = z;
+#pragma unroll
+    for (int k = 0; k < 7; k++) { R[0][k] = E.r[k]; R[2][k] = E.t[k]; }
+#pragma unroll
+    for (int k = 2; k < 6; k++) R[1][k] = E.s[k];
+    R[3][0] = T(1.0);
+#pragma unroll
+    for (int k = 1; k < 7; k++) R[3][k] = z;
+    mirror_row(L[0], L[6]); mirror_row(L[1], L[5]); mirror_row(L[2], L[4]);
+    mirror_row(R[0], R[6]); mirror_row(R[1], R[5]); mirror_row(R[2], R[4]);
+}
+
+// Fast-speed quantities shared by the Alfven/entropy and Miyoshi systems
+// (mhd_eigen.h:206-212, :337-343).
+template <class T> MLAU_HD T fast_speed2(T ro, T bx, T by, T bz, T pr, T gamma)
+{
     const T iro = T(1.0) / ro;
     const T cs2 = gamma * pr * iro;
-    const T ca2 = bn * bn * iro;
+    const T ca2 = bx * bx * iro;
     const T ct2 = (by * by + bz * bz) * iro;
     const T cb2 = cs2 + ca2 + ct2;
-    const T cf2 = T(0.5) * (cb2 + tsqrt(tabs(cb2 * cb2 - T(4.0) * cs2 * ca2)));
+    return T(0.5) * (cb2 + tsqrt(tabs(cb2 * cb2 - T(4.0) * cs2 * ca2)));
+}
+
+// mhd_eigen_ae (mhd_eigen.h:326-453): Alfven and entropy modes.
+template <class T>
+MLAU_HD void eigen_ae_dense(T ro, T vx, T vy, T vz, T bx, T by, T bz, T pr, T gamma, T al[7],
+                            T L[7][7], T R[7][7])
+{
+    (void)vx; (void)vy; (void)vz; (void)al;
+    const T cf2 = fast_speed2(ro, bx, by, bz, pr, gamma);
+    const T sro = tsqrt(ro);
+    const T isroh = T(0.5) / sro;
+    const T icf2 = T(1.0) / cf2;
+    const T byh = T(0.5) * by, bzh = T(0.5) * bz;
+    const T z = T(0), one = T(1.0), h = T(0.5);
+    const T l[7][7] = {{z, +one, z, z, z, z, z},
+                       {cf2, z, z, z, -by, -bz, T(-1.0)},
+                       {z, z, z, z, +by, +bz, +one},
+                       {z, z, +sro, z, +one, z, z},
+                       {z, z, +sro, z, T(-1.0), z, z},
+                       {z, z, z, +sro, z, +one, z},
+                       {z, z, z, +sro, z, T(-1.0), z}};
+    const T r[7][7] = {{z, +one, z, z, z, z, z},
+                       {+icf2, z, z, z, z, z, z},
+                       {+icf2, z, z, z, z, z, +one},
+                       {z, z, +isroh, z, +h, z, -byh},
+                       {z, z, +isroh, z, T(-0.5), z, +byh},
+                       {z, z, z, +isroh, z, +h, -bzh},
+                       {z, z, z, +isroh, z, T(-0.5), +bzh}};
+#pragma unroll
+    for (int n = 0; n < 7; n++)
+#pragma unroll
+        for (int k = 0; k < 7; k++) { L[n][k] = l[n][k]; R[n][k] = r[n][k]; }
+}
+
+// mhd_eigen_mi (mhd_eigen.h:194-324): Miyoshi's fast and Alfven modes (the
+// slow mode is ignored).
+template <class T>
+MLAU_HD void eigen_mi_dense(T ro, T vx, T vy, T vz, T bx, T by, T bz, T pr, T gamma, T al[7],
+                            T L[7][7], T R[7][7])
+{
+    (void)vx; (void)vy; (void)vz; (void)al;
+    const T cf2 = fast_speed2(ro, bx, by, bz, pr, gamma);
     const T cf = tsqrt(cf2);
     const T rcf = ro * cf;
     const T sro = tsqrt(ro);
@@ -448,21 +593,37 @@ MLAU_HD void reconst_miyoshi(int odr, const T q[7][5], T bn, T gamma, T ul[7], T
     const T ircfh = T(0.5) / rcf;
     const T byh = T(0.5) * by, bzh = T(0.5) * bz;
     const T z = T(0), one = T(1.0);
-    // left rows l[n][k] and right columns r[k][n] of the reference
-    const T L[7][7] = {{z, -rcf, z, z, +by, +bz, +one},
+    const T l[7][7] = {{z, -rcf, z, z, +by, +bz, +one},
                        {cf2, z, z, z, -by, -bz, -one},
                        {z, +rcf, z, z, +by, +bz, +one},
                        {z, z, +sro, z, +one, z, z},
                        {z, z, +sro, z, -one, z, z},
                        {z, z, z, +sro, z, +one, z},
                        {z, z, z, +sro, z, -one, z}};
-    const T R[7][7] = {{+icf2h, -ircfh, z, z, z, z, T(0.5)},
+    const T r[7][7] = {{+icf2h, -ircfh, z, z, z, z, T(0.5)},
                        {+icf2, z, z, z, z, z, z},
                        {+icf2h, +ircfh, z, z, z, z, T(0.5)},
                        {z, z, +isroh, z, T(0.5), z, -byh},
                        {z, z, +isroh, z, T(-0.5), z, +byh},
                        {z, z, z, +isroh, z, T(0.5), -bzh},
                        {z, z, z, +isroh, z, T(-0.5), +bzh}};
+#pragma unroll
+    for (int n = 0; n < 7; n++)
+#pragma unroll
+        for (int k = 0; k < 7; k++) { L[n][k] = l[n][k]; R[n][k] = r[n][k]; }
+}
+
+// Fast + Alfven projection of Miyoshi (mhd_m_reconst with mhd_eigen_mi,
+// mhd_eigen.h:194-324, 532-607; the slow mode is ignored), the header's
+// alternative to the full system.  The reference multiplies the dense 7x7
+// rows, zeros included, in index order; so does this (the zero products
+// decide signed zeros).
+template <class T>
+MLAU_HD void reconst_miyoshi(int odr, const T q[7][5], T bn, T gamma, T ul[7], T ur[7])
+{
+    T al[7], L[7][7], R[7][7];
+    eigen_mi_dense(q[0][2], q[1][2], q[2][2], q[3][2], bn, q[4][2], q[5][2], q[6][2], gamma, al,
+                   L, R);
     T w[7][5];
 #pragma unroll
     for (int n = 0; n < 7; n++)
@@ -497,6 +658,67 @@ MLAU_HD void reconst_face(int odr, int eig, T mach2, const T q[7][5], T bn, T ga
         else reconst_full(odr, q, bn, gamma, ul, ur);
     } else {
         reconst_alfven(odr, q, bn, gamma, ul, ur);
+    }
+}
+
+// Characteristic reconstruction of an s-point stencil with any eigen-system
+// and any face interpolation, as include/mhd_eigen.h's mhd_c_reconst /
+// mhd_a_reconst / mhd_m_reconst compute it (:455-684): eigenvectors of the
+// centre point s/2 (identity where the system leaves an entry unset), dense
+// projection w = L q, func_lr on each characteristic field, back-projection
+// with R, then the exact-zero guard on the transverse velocities and fields.
+// eig: eigen_st_dense, eigen_ae_dense or eigen_mi_dense.  s is at most
+// kMaxStencil (the drivers use 5); a larger s returns NaN faces.
+constexpr int kMaxStencil = 8;
+
+template <class T, class EIG, class LR>
+MLAU_HD void reconst_dense(EIG eig, const T *ro, const T *vx, const T *vy, const T *vz,
+                           const T *by, const T *bz, const T *pr, T bx, T gamma, int s, T *ul,
+                           T *ur, LR func_lr)
+{
+    if (s < 1 || s > kMaxStencil) {
+        for (int n = 0; n < 7; n++) { ul[n] = T(NAN); ur[n] = T(NAN); }
+        return;
+    }
+    T al[7], L[7][7], R[7][7];
+    for (int n = 0; n < 7; n++)
+        for (int k = 0; k < 7; k++) { L[n][k] = (n == k) ? T(1.0) : T(0); R[n][k] = L[n][k]; }
+    const int c = s / 2;
+    eig(ro[c], vx[c], vy[c], vz[c], bx, by[c], bz[c], pr[c], gamma, al, L, R);
+    T w[7][kMaxStencil], wl[7], wr[7];
+    for (int m = 0; m < s; m++)
+        for (int n = 0; n < 7; n++)
+            w[n][m] = (+L[n][0] * ro[m] + L[n][1] * vx[m] + L[n][2] * vy[m] + L[n][3] * vz[m]
+                       + L[n][4] * by[m] + L[n][5] * bz[m] + L[n][6] * pr[m]);
+    for (int n = 0; n < 7; n++) func_lr(&w[n][0], &wl[n], &wr[n]);
+    for (int n = 0; n < 7; n++)
+        ul[n] = R[0][n] * wl[0] + R[1][n] * wl[1] + R[2][n] * wl[2] + R[3][n] * wl[3]
+                + R[4][n] * wl[4] + R[5][n] * wl[5] + R[6][n] * wl[6];
+    for (int n = 0; n < 7; n++)
+        ur[n] = R[0][n] * wr[0] + R[1][n] * wr[1] + R[2][n] * wr[2] + R[3][n] * wr[3]
+                + R[4][n] * wr[4] + R[5][n] * wr[5] + R[6][n] * wr[6];
+    const T *tr[5] = {vx, vy, vz, by, bz};
+    for (int k = 0; k < 5; k++) {
+        bool z = true;
+        for (int m = 0; m < s; m++) z = z && (tr[k][m] == T(0));
+        if (z) { ul[k + 1] = T(0); ur[k + 1] = T(0); }
+    }
+}
+
+// mhd_reconst (mhd_eigen.h:686-724): func_lr on the primitives themselves.
+template <class T, class LR>
+MLAU_HD void reconst_prim(const T *ro, const T *vx, const T *vy, const T *vz, const T *by,
+                          const T *bz, const T *pr, int s, T *ul, T *ur, LR func_lr)
+{
+    if (s < 1 || s > kMaxStencil) {
+        for (int n = 0; n < 7; n++) { ul[n] = T(NAN); ur[n] = T(NAN); }
+        return;
+    }
+    const T *q[7] = {ro, vx, vy, vz, by, bz, pr};
+    T w[kMaxStencil];
+    for (int n = 0; n < 7; n++) {
+        for (int m = 0; m < s; m++) w[m] = q[n][m];
+        func_lr(w, &ul[n], &ur[n]);
     }
 }
 
@@ -985,4 +1207,29 @@ MLAU_HD void riemann_jumps(int which, const T *L, const T *R, T bn, T gamma, T d
     }
 }
 
+// hall_flux_lf (mhd_flux.h:734-766): Lax-Friedrichs fluxes of the Hall
+// term's tangential B and energy; v is the Hall velocity, smax the maximum
+// speed.  No driver of the ideal step calls it.
+template <class T>
+MLAU_HD void hall_lf(T vnl, T vtl, T vul, T btl, T bul, T vnr, T vtr, T vur, T btr, T bur, T bnc,
+                     T smax, T *fbt, T *fbu, T *fen)
+{
+    const T pml = T(0.5) * (bnc * bnc + btl * btl + bul * bul);
+    const T vbl = vnl * bnc + vtl * btl + vul * bul;
+    const T pmr = T(0.5) * (bnc * bnc + btr * btr + bur * bur);
+    const T vbr = vnr * bnc + vtr * btr + vur * bur;
+    const T fbtl = btl * vnl - bnc * vtl, fbul = bul * vnl - bnc * vul;
+    const T fenl = T(2.0) * pml * vnl - bnc * vbl;
+    const T fbtr = btr * vnr - bnc * vtr, fbur = bur * vnr - bnc * vur;
+    const T fenr = T(2.0) * pmr * vnr - bnc * vbr;
+    *fbt = T(0.5) * (fbtl + fbtr - smax * (btr - btl));
+    *fbu = T(0.5) * (fbul + fbur - smax * (bur - bul));
+    *fen = T(0.5) * (fenl + fenr - smax * (pmr - pml));
+}
+
 }  // namespace mlau
+
+#ifdef MLAU_POINT_DIAG_PUSHED
+#pragma GCC diagnostic pop
+#undef MLAU_POINT_DIAG_PUSHED
+#endif

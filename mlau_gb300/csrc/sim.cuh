@@ -28,6 +28,12 @@ struct Geometry {
 
 struct SplitFields;  // FP32-split workspace (split3d.cu)
 
+// The two FP32-split forms share the workspace and the kernels.
+inline bool is_split(int precision)
+{
+    return precision == MLAU_FP32_SPLIT || precision == MLAU_FP32_SPLIT_F64;
+}
+
 struct Sim {
     Geometry g;
     double gamma;

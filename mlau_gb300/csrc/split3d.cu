@@ -84,6 +84,7 @@ struct SplitFields {
     int ntiles[3] = {};
     int nblocks[3] = {};    // persistent grid per sweep
     int spec = 0;           // sweep instance: 0 run-time scheme, 1 WCNS4 + MLAU, 2 WCNS4 + LHLLD
+    int f64 = 0;            // state arithmetic in FP64 (MLAU_FP32_SPLIT_F64), else float-float
     int *d_err = nullptr;   // set when a bounded wait gave up
     // host-array steps (split3d_step_host): copy stream and slab events
     cudaStream_t cs = nullptr;
@@ -139,8 +140,13 @@ __device__ __forceinline__ ff face2cen_ff(int odr, const double b[4])
     return ff_scale(ff_sub(ff_mul_f(ff_add(f1, f2), 9.0f), ff_add(f0, f3)), 0.0625f);
 }
 
+// F64: pressure recovery and cell B in FP64 arithmetic (the split form with
+// FP64 kept for the state arithmetic) instead of float-float; the primitives
+// then leave as the (hi, lo) splits of their FP64 values, velocities included.
+template <bool F64>
 __global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, int save_u0, int k0)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, double gm1d, float gamma_f,
+        int save_u0, int k0)
 {
     int i, j, k;
     if (!plane_cell(d, i, j, k, k0)) return;
@@ -157,6 +163,35 @@ ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, float gamma_f, 
         for (int m = 0; m < 4; m++) bs[a][m] = f.s[5 + a][w + (m - 1) * st[a]];
 #pragma unroll
     for (int v = 0; v < 8; v++) u[v] = f.s[v][s];
+    if constexpr (F64) {
+        // p = (gamma-1)(E - rho v^2/2 - B^2/2) and cell B in FP64
+        const double ro = u[0], iro = 1.0 / ro;
+        const double cx = face2cen(odr, bs[0][0], bs[0][1], bs[0][2], bs[0][3]);
+        const double cy = face2cen(odr, bs[1][0], bs[1][1], bs[1][2], bs[1][3]);
+        const double cz = face2cen(odr, bs[2][0], bs[2][1], bs[2][2], bs[2][3]);
+        const double vx = u[1] * iro, vy = u[2] * iro, vz = u[3] * iro;
+        const double pr = gm1d * (u[4] - 0.5 * (ro * (vx * vx + vy * vy + vz * vz)
+                                                + (cx * cx + cy * cy + cz * cz)));
+        const float2 ro2 = split2(ro), vx2 = split2(vx), vy2 = split2(vy), vz2 = split2(vz);
+        const float2 pr2 = split2(pr);
+        g.q[0][sp] = ro2;
+        g.q[1][sp] = vx2;
+        g.q[2][sp] = vy2;
+        g.q[3][sp] = vz2;
+        g.q[4][sp] = split2(cx);
+        g.q[5][sp] = split2(cy);
+        g.q[6][sp] = split2(cz);
+        g.q[7][sp] = pr2;
+        g.bf[0][sp] = to_f32(u[5]);
+        g.bf[1][sp] = to_f32(u[6]);
+        g.bf[2][sp] = to_f32(u[7]);
+        if (save_u0)
+#pragma unroll
+            for (int v = 0; v < 8; v++) f.u0[v][s] = u[v];
+        const float fx = vx2.x + vx2.y, fy = vy2.x + vy2.y, fz = vz2.x + vz2.y;
+        g.m2[sp] = (fx * fx + fy * fy + fz * fz) / (gamma_f * (pr2.x + pr2.y) / (ro2.x + ro2.y));
+        return;
+    }
     const ff cx = face2cen_ff(odr, bs[0]);
     const ff cy = face2cen_ff(odr, bs[1]);
     const ff cz = face2cen_ff(odr, bs[2]);
@@ -648,8 +683,26 @@ __device__ __forceinline__ void ld4(float v[4], const float *f, long long s, lon
     for (int m = 0; m < 4; m++) v[m] = __ldg(f + s + (m - 1) * st);
 }
 
+// FP64 difference of the FP32 edge EMFs f0..f3 along one axis (the values
+// converted exactly), without the 1/24 of the 4th-order stencil.
+__device__ __forceinline__ double df_f64(int odr, const float e[4])
+{
+    const double e0 = to_f64(e[0]), e1 = to_f64(e[1]), e2 = to_f64(e[2]), e3 = to_f64(e[3]);
+    if (lin_odr(odr) <= 2) return e2 - e1;
+    return 27.0 * (e2 - e1) - (e3 - e0);
+}
+
+// F64: the RK combine and the CT curl in FP64 arithmetic (the split form
+// with FP64 kept for the state arithmetic); the flux divergence is formed in
+// FP32 as in the float-float form.  rd: (ra, rb) and (dt/dx, dt/dy, dt/dz)
+// times the stencil's 1/24, as doubles.
+struct RkF64 {
+    double ra, rb, ddx, ddy, ddz;
+};
+
+template <bool F64>
 __global__ void __launch_bounds__(128)
-ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, float dtdx, float dtdy,
+ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, RkF64 rd, float dtdx, float dtdy,
           float dtdz, float2 ddx2, float2 ddy2, float2 ddz2, int k0)
 {
     const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
@@ -681,25 +734,43 @@ ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, float dtdx, floa
     }
     // arithmetic
     double out[8];
+    if constexpr (F64) {
 #pragma unroll
-    for (int v = 0; v < 5; v++) {
-        const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
-                          + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
-                          + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
-        // the first stage is u - div: one FP64 addition beats its float-float form
-        out[v] = rk.first ? u[v] - to_f64(div) : rk_ff(rk, u0[v], ff_add_f(ff_from(u[v]), -div));
+        for (int v = 0; v < 5; v++) {
+            const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
+                              + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
+                              + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
+            const double w = u[v] - to_f64(div);
+            out[v] = rk.first ? w : rd.ra * u0[v] + rd.rb * w;
+        }
+        const double b5 = u[5] - rd.ddy * df_f64(odr, ezy) + rd.ddz * df_f64(odr, eyz);
+        const double b6 = u[6] - rd.ddz * df_f64(odr, exz) + rd.ddx * df_f64(odr, ezx);
+        const double b7 = u[7] - rd.ddx * df_f64(odr, eyx) + rd.ddy * df_f64(odr, exy);
+        out[5] = rk.first ? b5 : rd.ra * u0[5] + rd.rb * b5;
+        out[6] = rk.first ? b6 : rd.ra * u0[6] + rd.rb * b6;
+        out[7] = rk.first ? b7 : rd.ra * u0[7] + rd.rb * b7;
+    } else {
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
+                              + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
+                              + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
+            // the first stage is u - div: one FP64 addition beats its float-float form
+            out[v] = rk.first ? u[v] - to_f64(div)
+                              : rk_ff(rk, u0[v], ff_add_f(ff_from(u[v]), -div));
+        }
+        // CT curl in float-float: the differences of the FP32 edge EMFs are
+        // exact, so the discrete divergence of the B increment cancels to the
+        // float-float round-off (in FP32, 27*(E2-E1) alone would need more than
+        // 24 bits).  ddx2 etc. carry the stencil's 1/24 when odr > 2.
+        const ff ddx = {ddx2.x, ddx2.y}, ddy = {ddy2.x, ddy2.y}, ddz = {ddz2.x, ddz2.y};
+        out[5] = rk_ff(rk, u0[5], ff_add(ff_sub(ff_from(u[5]), ff_mul(ddy, df_ff(odr, ezy))),
+                                         ff_mul(ddz, df_ff(odr, eyz))));
+        out[6] = rk_ff(rk, u0[6], ff_add(ff_sub(ff_from(u[6]), ff_mul(ddz, df_ff(odr, exz))),
+                                         ff_mul(ddx, df_ff(odr, ezx))));
+        out[7] = rk_ff(rk, u0[7], ff_add(ff_sub(ff_from(u[7]), ff_mul(ddx, df_ff(odr, eyx))),
+                                         ff_mul(ddy, df_ff(odr, exy))));
     }
-    // CT curl in float-float: the differences of the FP32 edge EMFs are
-    // exact, so the discrete divergence of the B increment cancels to the
-    // float-float round-off (in FP32, 27*(E2-E1) alone would need more than
-    // 24 bits).  ddx2 etc. carry the stencil's 1/24 when odr > 2.
-    const ff ddx = {ddx2.x, ddx2.y}, ddy = {ddy2.x, ddy2.y}, ddz = {ddz2.x, ddz2.y};
-    out[5] = rk_ff(rk, u0[5], ff_add(ff_sub(ff_from(u[5]), ff_mul(ddy, df_ff(odr, ezy))),
-                                     ff_mul(ddz, df_ff(odr, eyz))));
-    out[6] = rk_ff(rk, u0[6], ff_add(ff_sub(ff_from(u[6]), ff_mul(ddz, df_ff(odr, exz))),
-                                     ff_mul(ddx, df_ff(odr, ezx))));
-    out[7] = rk_ff(rk, u0[7], ff_add(ff_sub(ff_from(u[7]), ff_mul(ddx, df_ff(odr, eyx))),
-                                     ff_mul(ddy, df_ff(odr, exy))));
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
     const int js[3] = {j, j < 2 * d.oy ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -886,6 +957,7 @@ int split3d_alloc(Sim *s)
     // the sweeps read the arrays' ghost rows too: start from zeros
     for (int v = 0; v < 8; v++) MLAU_CUDA(cudaMemset(g.q[v], 0, sizeof(float2) * np));
     sf.spec = (s->odr == 4 && s->flux == FLUX_MLAU) ? 1 : (s->odr == 4 && s->flux == FLUX_LHLLD) ? 2 : 0;
+    sf.f64 = s->precision == MLAU_FP32_SPLIT_F64;
     int r2 = setup_sweep<0>(s, sf);
     if (!r2) r2 = setup_sweep<1>(s, sf);
     if (!r2) r2 = setup_sweep<2>(s, sf);
@@ -937,9 +1009,10 @@ struct StepCtx {
     // primitive recovery of planes [k0, k0 + nk)
     void prim(int rk, int k0, int nk) const
     {
-        ks_prim<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->f, s->sp->p, d, s->odr,
-                                                      host_ff(s->gamma - 1), (float)s->gamma,
-                                                      rk == 0, k0);
+        auto kern = s->sp->f64 ? ks_prim<true> : ks_prim<false>;
+        kern<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->f, s->sp->p, d, s->odr,
+                                                   host_ff(s->gamma - 1), s->gamma - 1,
+                                                   (float)s->gamma, rk == 0, k0);
     }
     void aux() const { ks_aux<<<cg, cb, 0, s->stream>>>(s->sp->p, d); }
     void sweeps() const
@@ -960,8 +1033,10 @@ struct StepCtx {
         const double ra = t[rk][0], rb = t[rk][1];
         const double c24 = lin_odr(s->odr) > 2 ? 1.0 / 24.0 : 1.0;
         const RkFF c{host_ff(ra), host_ff(rb), ra == 0.0 && rb == 1.0};
-        ks_update<<<dim3(ug.x, ug.y, nk), cb, 0, s->stream>>>(
-            s->f, s->sp->p, d, s->odr, c, (float)(dt / G.dx), (float)(dt / G.dy),
+        const RkF64 c64{ra, rb, dt / G.dx * c24, dt / G.dy * c24, dt / G.dz * c24};
+        auto kern = s->sp->f64 ? ks_update<true> : ks_update<false>;
+        kern<<<dim3(ug.x, ug.y, nk), cb, 0, s->stream>>>(
+            s->f, s->sp->p, d, s->odr, c, c64, (float)(dt / G.dx), (float)(dt / G.dy),
             (float)(dt / G.dz), host_ff(dt / G.dx * c24), host_ff(dt / G.dy * c24),
             host_ff(dt / G.dz * c24), k0);
     }

@@ -211,6 +211,7 @@ class Ref:
     """ctypes binding of a reference-driver variant built into oracle/_ref."""
 
     _libs: dict = {}
+    HEADERS = "ref"
 
     @staticmethod
     def available() -> bool:
@@ -220,7 +221,8 @@ class Ref:
     def _get(cls, dim, odr, flux, nrk, bc="open", eig="full"):
         key = (dim, odr, flux, nrk, bc if dim == 1 else "", eig)
         if key not in cls._libs:
-            lib = C.CDLL(build.build_ref_variant(dim, odr, flux, nrk, bc, eig == "miyoshi"))
+            lib = C.CDLL(build.build_ref_variant(dim, odr, flux, nrk, bc, eig == "miyoshi",
+                                                 headers=cls.HEADERS))
             d, i = C.c_double, C.c_int
             if dim == 1:
                 lib.ref_step_1d.argtypes = [_dp] * 7 + [d, d, d, i, i, d]
@@ -276,6 +278,15 @@ class Ref:
         nx = s["ro"].shape[0]
         cls._get(1, odr, _flux_id(flux), nrk, bc, eig).ref_step_1d(
             *[s[k] for k in ("ro", "mx", "my", "mz", "en", "by", "bz")], bx, dt, dx, nx, off, gamma)
+
+
+class RefOnMlauPoint(Ref):
+    """The reference's own drivers compiled unchanged against this library's
+    include/mlau_point.h in place of the reference's point-function headers
+    (funcs.h, interp.h, mhd_eigen.h, mhd_flux.h)."""
+
+    _libs: dict = {}
+    HEADERS = "mlau"
 
 
 class RefMRX:

@@ -26,7 +26,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("MLAU_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: MLAU_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository's root
+REF_ROOT = os.environ.get("MLAU_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 
 FLUX_NAMES = {0: "mlau", 1: "lhlld", 2: "hlld", 3: "roe"}
 CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
@@ -88,18 +91,40 @@ def _patch_driver(text: str, odr: int, flux: int, nrk: int, miyoshi: bool = Fals
     return text
 
 
+REPO_INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+POINT_HEADERS = ("funcs.h", "interp.h", "mhd_eigen.h", "mhd_flux.h")
+
+
+def point_shim_dir() -> str:
+    """A directory of one-line headers named as the reference's point-function
+    headers, each including this library's include/mlau_point.h: put first on
+    the include path, it swaps the reference's point functions for the
+    library's in a reference driver compiled unchanged."""
+    d = os.path.join(REF_OUT, "shim")
+    os.makedirs(d, exist_ok=True)
+    for h in POINT_HEADERS:
+        path = os.path.join(d, h)
+        text = '#include "mlau_point.h"\n'
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as fh:
+                fh.write(text)
+    return d
+
+
 def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
-                      bc: str = "open", miyoshi: bool = False) -> str:
+                      bc: str = "open", miyoshi: bool = False, headers: str = "ref") -> str:
     """Compile one scheme variant of the reference driver; return the .so path.
 
     dim 3: 3D/MPI/OTvortex/{mhd_fd_ct_3d.c,boundary.c}
     dim 2: 2D/SERIAL/OTvortex/{mhd_fd_ct_2d.c,boundary.c}
     dim 1: 1D/SERIAL/shock/{mhd_fd4c_1d.c,openbc1d_mhd.c} (bc="open") or
            1D/SERIAL/wave/{mhd_fd4c_1d.c,prdc_1d.c} (bc="periodic")
+    headers "mlau": the same driver sources compiled against include/mlau_point.h
+    in place of the reference's include/{funcs,interp,mhd_eigen,mhd_flux}.h.
     """
     if not reference_available():
         raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
-    name = _variant_name(dim, odr, flux, nrk, bc, miyoshi)
+    name = _variant_name(dim, odr, flux, nrk, bc, miyoshi) + ("_mlauhdr" if headers == "mlau" else "")
     out = os.path.join(REF_OUT, f"lib{name}.so")
     if os.path.exists(out):
         return out
@@ -120,9 +145,38 @@ def build_ref_variant(dim: int, odr: int = 4, flux: int = 0, nrk: int = 3,
         fh.write(patched)
     srcs = [drv_copy] + [os.path.join(REF_ROOT, d, e) for e in extra]
     tmp = out + f".tmp{os.getpid()}"
-    cmd = ["g++", "-x", "c++", *CFLAGS, f"-DREF_DIM={dim}",
+    inc = ["-I" + point_shim_dir(), "-I" + REPO_INCLUDE] if headers == "mlau" else []
+    cmd = ["g++", "-x", "c++", *CFLAGS, f"-DREF_DIM={dim}", *inc,
            "-I" + os.path.join(REF_ROOT, "include"), "-I" + os.path.join(HERE, "ref_stub"),
            "-o", tmp, *srcs, os.path.join(HERE, "ref_harness.cpp"), "-lm"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+    os.replace(tmp, out)
+    return out
+
+
+def build_point_harness(headers: str = "ref", out: str | None = None) -> str:
+    """Compile oracle/point_harness.cpp against the reference's point-function
+    headers (headers "ref", into oracle/_ref/libpoint_ref.so; needs the
+    reference tree) or against include/mlau_point.h (headers "mlau", into
+    `out`); return the .so path."""
+    src = os.path.join(HERE, "point_harness.cpp")
+    if headers == "ref":
+        if not reference_available():
+            raise FileNotFoundError(f"reference tree not found at {REF_ROOT}")
+        out = out or os.path.join(REF_OUT, "libpoint_ref.so")
+        inc = ["-DMLAU_POINT_REF", "-I" + os.path.join(REF_ROOT, "include")]
+    else:
+        out = out or os.path.join(BUILD, "libpoint_mlau.so")
+        inc = ["-I" + REPO_INCLUDE]
+    deps = [src] + ([os.path.join(REPO_INCLUDE, "mlau_point.h"),
+                     os.path.join(os.path.dirname(HERE), "mlau_gb300", "csrc", "point.cuh")]
+                    if headers != "ref" else [])
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+        return out
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", *inc,
+           "-o", tmp, src, "-lm"]
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
     os.replace(tmp, out)
     return out

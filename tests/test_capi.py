@@ -65,6 +65,11 @@ def test_create_rejects_bad_geometry(gpu_lib):
     assert rc == -1 and "gamma" in gpu_lib.last_error()
     rc = L.mlau_sim_create(C.byref(h), 1, 64, 1, 1, 4, 0, 0, 1.0, 1.0, 1.0, 2.0, 2, 0, 3, 1)
     assert rc == -1 and "precision" in gpu_lib.last_error()
+    # ghost depth 3: the update's 4-point difference would read a face no
+    # flux kernel writes (the reference fixes the depth at 4)
+    for dim, g in ((1, (64, 1, 1, 3, 0, 0)), (2, (32, 32, 1, 3, 4, 0)), (3, (32, 32, 32, 4, 4, 3))):
+        rc = L.mlau_sim_create(C.byref(h), dim, *g, 1.0, 1.0, 1.0, 5 / 3, 4, 0, 3, 0)
+        assert rc == -1 and "ghost depth >= 4" in gpu_lib.last_error()
 
 
 def test_set_scheme_validation(gpu_lib):

@@ -209,7 +209,7 @@ def test_port_zero_guard_2d(port):
     assert not st["mz"].any() and not st["bz"].any()
 
 
-def test_port_thread_count_independent(port):
+def test_port_thread_count_independent(port, tmp_path):
     """The step has no reductions: results do not depend on thread count."""
     import os
     import subprocess
@@ -221,11 +221,10 @@ def test_port_thread_count_independent(port):
     ) % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     outs = []
     for t in ("1", "4"):
-        path = f"/tmp/mlau_thr_{os.getpid()}_{t}.npy"
+        path = str(tmp_path / f"thr_{t}.npy")
         subprocess.run([sys.executable, "-c", code, path], check=True,
                        env={**os.environ, "OMP_NUM_THREADS": t})
         outs.append(np.load(path))
-        os.remove(path)
     assert np.array_equal(outs[0], outs[1])
 
 
