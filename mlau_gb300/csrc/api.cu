@@ -110,7 +110,7 @@ static int check_geometry(int dim, int nx, int ny, int nz, int ox, int oy, int o
 int launches_per_step(const Sim *s)
 {
     // kernels per RK stage (device-to-device copies are not counted)
-    if (s->sp) return s->nrk * 7;
+    if (s->sp) return s->nrk * (s->walls3d ? 9 : 7);
     if (s->g.dim == 3) return s->nrk * (s->walls3d ? 12 : 10);
     if (s->g.dim == 2) return s->nrk * (s->walls2d ? 10 : 8);
     return s->nrk * 4 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
@@ -281,10 +281,6 @@ int mlau_sim_set_bc_3d(mlau_sim *s, const int *dnx, const int *dny, const int *d
             return MLAU_ERR_ARG;
         }
         walls = walls || nz != 0;
-    }
-    if (walls && s->precision != MLAU_FP64) {
-        set_error("non-periodic 3D boundaries are built for the FP64 step only");
-        return MLAU_ERR_ARG;
     }
     if (std::memcmp(s->bc3.x, dnx, sizeof(s->bc3.x)) || std::memcmp(s->bc3.y, dny, sizeof(s->bc3.y)) ||
         std::memcmp(s->bc3.z, dnz, sizeof(s->bc3.z)))
@@ -600,7 +596,7 @@ void report(const char *who)
 int run_dropin(mlau_sim *c, double *const *h, double dt)
 {
     // FP32-split: the host link's copies overlap the step where the data allow
-    if (c->sp) return split3d_step_host(c, dt, h);
+    if (c->sp && !c->walls3d) return split3d_step_host(c, dt, h);
     int rc = mlau_sim_upload(c, (const double *const *)h);
     if (rc == MLAU_OK) rc = mlau_sim_step(c, dt, 1);
     if (rc == MLAU_OK) rc = mlau_sim_download(c, h);

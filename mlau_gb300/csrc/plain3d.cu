@@ -350,6 +350,17 @@ int plain3d_alloc(Sim *s)
     return rc ? MLAU_ERR_NOMEM : MLAU_OK;
 }
 
+// Ghost fill of the FP64 state with the simulation's 3D tables (also the
+// last act of an FP32-split stage with non-periodic tables).
+int plain3d_fill_ghosts(Sim *s)
+{
+    const Geometry &g = s->g;
+    const Dims d{g.nx, g.ny, g.nz, g.ox, g.oy, g.oz};
+    const Box all{0, 0, 0, g.nx, g.ny, g.nz};
+    k_bc3<<<blocks_for(all.count(), TPB), TPB, 0, s->stream>>>(s->f, d, all, s->bc3);
+    return MLAU_OK;
+}
+
 int plain3d_step(Sim *s, double dt)
 {
     const Geometry &g = s->g;

@@ -2,17 +2,21 @@
 // (3D/MPI/OTvortex/mhd_fd_ct_3d.c), with the arithmetic split by what needs
 // more than FP32:
 //
-//   float-float (~48 bits, FP32 pipe; the state is stored in FP64)
-//         the RK3 accumulation of flux differences into the conserved state,
-//         primitive recovery p = (gamma-1)(E - rho v^2/2 - B^2/2) and cell B
-//         (cancellation at low Mach and low beta), the CT curl update of face
-//         B (div B at round-off).
+//   FP64  the CT curl update of face B (div B at FP64 round-off); the state
+//         is stored in FP64.
+//   float-float (~48 bits, FP32 pipe)
+//         the RK3 accumulation of flux differences into the cell-centred
+//         state and primitive recovery p = (gamma-1)(E - rho v^2/2 - B^2/2)
+//         with cell B (cancellation at low Mach and low beta); FP64 in the
+//         MLAU_FP32_SPLIT_F64 form.
 //   FP32  characteristic reconstruction and the Riemann solver, the edge EMFs,
 //         the CT weights and shock sensors.
 //
 // On this part FP64 issues at 1/64 of the FP32 rate, so the 48-bit parts run
 // as float-float arithmetic (ff.cuh) rather than FP64: 10-20 FP32 operations
 // per FP64 one still leave the prep and update kernels near the memory roof.
+// Measured over 200 steps at 256^3 the float-float and FP64 forms of these
+// two parts give the same L1 error against the plain FP64 step.
 //
 // Reconstruction works on perturbations from the cell centre, q_m - q_c, and
 // WCNS/MUSCL/linear weights are translation invariant, so the face states
@@ -28,8 +32,8 @@
 //
 // Kernels per RK stage: prep (float-float primitive recovery -> float pairs),
 // aux (FP32 CT weights and shock sensors), one fused reconstruction + flux
-// kernel per direction, emf (FP32), update (float-float RK combine + CT curl +
-// periodic ghost images).
+// kernel per direction, emf (FP32), update (float-float RK combine, FP64 CT
+// curl, periodic ghost images).
 //
 // The fused sweep is a persistent kernel over tiles.  Each tile's inputs (the
 // 5-point stencils of eight float-pair arrays and four float arrays, halo
@@ -52,6 +56,8 @@
 #include <algorithm>
 
 namespace mlau {
+
+int plain3d_fill_ghosts(Sim *s);  // plain3d.cu: ghost fill of the FP64 state with the tables
 
 // Arrays staged for a sweep, in the sweep's rotated order: density, normal /
 // tangential / third velocity, the two tangential cell B components,
@@ -143,32 +149,47 @@ __device__ __forceinline__ ff face2cen_ff(int odr, const double b[4])
 // F64: pressure recovery and cell B in FP64 arithmetic (the split form with
 // FP64 kept for the state arithmetic) instead of float-float; the primitives
 // then leave as the (hi, lo) splits of their FP64 values, velocities included.
-template <bool F64>
+// WALLS: the boundary tables bc are not all periodic; each cell-B component
+// then reads its face stencil at its own boundary source, with its sign
+// (3D/MPI/OTvortex/mhd_fd_ct_3d.c:186-238, boundary.c:227-309).
+template <bool F64, bool WALLS>
 __global__ void __launch_bounds__(256)
-ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, double gm1d, float gamma_f,
-        int save_u0, int k0)
+ks_prim(PlainFields f, SplitPtrs g, Dims d, Bc3 bc, int odr, float2 gm1, double gm1d,
+        float gamma_f, int save_u0, int k0)
 {
     int i, j, k;
     if (!plane_cell(d, i, j, k, k0)) return;
     const long long sy = d.nx, sz = (long long)d.nx * d.ny;
-    const long long w = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
     const long long s = d.at(i, j, k), sp = d.ap(i, j, k);
     // loads first, so that they are in flight together (the kernel waits on
-    // memory otherwise); the face stencils are at the cell's boundary source w
+    // memory otherwise); the face stencils are at the cell's boundary source
+    long long w[3];
+    double gb[3] = {1.0, 1.0, 1.0};
+    if constexpr (WALLS) {
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            w[a] = d.at(bc_src(i, d.nx, d.ox, 0, bc.x[5 + a], &gb[a]),
+                        bc_src(j, d.ny, d.oy, 0, bc.y[5 + a], &gb[a]),
+                        bc_src(k, d.nz, d.oz, 0, bc.z[5 + a], &gb[a]));
+    } else {
+        w[0] = d.at(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
+        w[1] = w[0];
+        w[2] = w[0];
+    }
     double bs[3][4], u[8];
     const long long st[3] = {1, sy, sz};
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
-        for (int m = 0; m < 4; m++) bs[a][m] = f.s[5 + a][w + (m - 1) * st[a]];
+        for (int m = 0; m < 4; m++) bs[a][m] = f.s[5 + a][w[a] + (m - 1) * st[a]];
 #pragma unroll
     for (int v = 0; v < 8; v++) u[v] = f.s[v][s];
     if constexpr (F64) {
         // p = (gamma-1)(E - rho v^2/2 - B^2/2) and cell B in FP64
         const double ro = u[0], iro = 1.0 / ro;
-        const double cx = face2cen(odr, bs[0][0], bs[0][1], bs[0][2], bs[0][3]);
-        const double cy = face2cen(odr, bs[1][0], bs[1][1], bs[1][2], bs[1][3]);
-        const double cz = face2cen(odr, bs[2][0], bs[2][1], bs[2][2], bs[2][3]);
+        const double cx = gb[0] * face2cen(odr, bs[0][0], bs[0][1], bs[0][2], bs[0][3]);
+        const double cy = gb[1] * face2cen(odr, bs[1][0], bs[1][1], bs[1][2], bs[1][3]);
+        const double cz = gb[2] * face2cen(odr, bs[2][0], bs[2][1], bs[2][2], bs[2][3]);
         const double vx = u[1] * iro, vy = u[2] * iro, vz = u[3] * iro;
         const double pr = gm1d * (u[4] - 0.5 * (ro * (vx * vx + vy * vy + vz * vz)
                                                 + (cx * cx + cy * cy + cz * cz)));
@@ -192,9 +213,10 @@ ks_prim(PlainFields f, SplitPtrs g, Dims d, int odr, float2 gm1, double gm1d, fl
         g.m2[sp] = (fx * fx + fy * fy + fz * fz) / (gamma_f * (pr2.x + pr2.y) / (ro2.x + ro2.y));
         return;
     }
-    const ff cx = face2cen_ff(odr, bs[0]);
-    const ff cy = face2cen_ff(odr, bs[1]);
-    const ff cz = face2cen_ff(odr, bs[2]);
+    // a mirror's sign (+-1) flips both parts exactly
+    const ff cx = ff_scale(face2cen_ff(odr, bs[0]), (float)gb[0]);
+    const ff cy = ff_scale(face2cen_ff(odr, bs[1]), (float)gb[1]);
+    const ff cz = ff_scale(face2cen_ff(odr, bs[2]), (float)gb[2]);
     const double ro = u[0];
     // Velocities and the kinetic energy in FP32: rho v^2/2 enters the pressure
     // as an additive term, so its FP32 rounding (1e-7 of itself) stays below
@@ -252,7 +274,11 @@ __device__ __forceinline__ float ct_w(const float2 *va, const float2 *vb, const 
     return (a + 0.5f * eps) / (a + c + eps);
 }
 
-__global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d)
+// WALLS: each shock sensor is read at its own boundary source with its sign,
+// as the reference fills them (mhd_fd_ct_3d.c:367-376: dvx takes -dnxs[1]
+// along x, dvy -dnys[2] along y, dvz -dnzs[3] along z).
+template <bool WALLS>
+__global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d, Bc3 bc)
 {
     int i, j, k;
     if (!plane_cell(d, i, j, k)) return;
@@ -262,10 +288,27 @@ __global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d)
     g.ct[0][s] = (i >= 1 && j >= 1) ? ct_w(vx, vy, ro, g.bf[0], g.bf[1], s, sy, 1, sy, 1) : 0.5f;
     g.ct[1][s] = (j >= 1 && k >= 1) ? ct_w(vy, vz, ro, g.bf[1], g.bf[2], s, sz, sy, sz, sy) : 0.5f;
     g.ct[2][s] = (k >= 1 && i >= 1) ? ct_w(vz, vx, ro, g.bf[2], g.bf[0], s, sz, 1, 1, sz) : 0.5f;
-    const long long w = d.ap(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
-    g.dv[0][s] = fminf(qd(vx, w + 1, w), qd(vx, w, w - 1));
-    g.dv[1][s] = fminf(qd(vy, w + sy, w), qd(vy, w, w - sy));
-    g.dv[2][s] = fminf(qd(vz, w + sz, w), qd(vz, w, w - sz));
+    if constexpr (WALLS) {
+        double g0 = 1.0, g1 = 1.0, g2 = 1.0;
+        const long long w0 = d.ap(bc_src(i, d.nx, d.ox, 0, -bc.x[1], &g0),
+                                  bc_src(j, d.ny, d.oy, 0, bc.y[1], &g0),
+                                  bc_src(k, d.nz, d.oz, 0, bc.z[1], &g0));
+        const long long w1 = d.ap(bc_src(i, d.nx, d.ox, 0, bc.x[2], &g1),
+                                  bc_src(j, d.ny, d.oy, 0, -bc.y[2], &g1),
+                                  bc_src(k, d.nz, d.oz, 0, bc.z[2], &g1));
+        const long long w2 = d.ap(bc_src(i, d.nx, d.ox, 0, bc.x[3], &g2),
+                                  bc_src(j, d.ny, d.oy, 0, bc.y[3], &g2),
+                                  bc_src(k, d.nz, d.oz, 0, -bc.z[3], &g2));
+        g.dv[0][s] = (float)g0 * fminf(qd(vx, w0 + 1, w0), qd(vx, w0, w0 - 1));
+        g.dv[1][s] = (float)g1 * fminf(qd(vy, w1 + sy, w1), qd(vy, w1, w1 - sy));
+        g.dv[2][s] = (float)g2 * fminf(qd(vz, w2 + sz, w2), qd(vz, w2, w2 - sz));
+    } else {
+        const long long w =
+            d.ap(wrap_idx(i, d.nx, d.ox), wrap_idx(j, d.ny, d.oy), wrap_idx(k, d.nz, d.oz));
+        g.dv[0][s] = fminf(qd(vx, w + 1, w), qd(vx, w, w - 1));
+        g.dv[1][s] = fminf(qd(vy, w + sy, w), qd(vy, w, w - sy));
+        g.dv[2][s] = fminf(qd(vz, w + sz, w), qd(vz, w, w - sz));
+    }
 }
 
 // --- fused reconstruction + Riemann flux along axis D ----------------------
@@ -654,17 +697,6 @@ __global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr)
 // registers first (read-only data through the non-coherent path), and the
 // arithmetic follows.
 
-// Float-float difference of the FP32 edge EMFs f0..f3 along one axis, without
-// the 1/24 of the 4th-order stencil (folded into dt/dx by the caller): the
-// differences of two floats are exact as float-float, and so is 27 times one,
-// so the discrete divergence of the curl cancels to the float-float
-// round-off.
-__device__ __forceinline__ ff df_ff(int odr, const float e[4])
-{
-    if (lin_odr(odr) <= 2) return ff_two_sum(e[2], -e[1]);
-    return ff_sub(ff_mul_f(ff_two_sum(e[2], -e[1]), 27.0f), ff_two_sum(e[3], -e[0]));
-}
-
 // The RK combine ra u0 + rb u in float-float (ra = 0, rb = 1 at the first stage).
 struct RkFF {
     float2 ra, rb;
@@ -692,10 +724,11 @@ __device__ __forceinline__ double df_f64(int odr, const float e[4])
     return 27.0 * (e2 - e1) - (e3 - e0);
 }
 
-// F64: the RK combine and the CT curl in FP64 arithmetic (the split form
-// with FP64 kept for the state arithmetic); the flux divergence is formed in
-// FP32 as in the float-float form.  rd: (ra, rb) and (dt/dx, dt/dy, dt/dz)
-// times the stencil's 1/24, as doubles.
+// F64: the RK combine of the cell-centred variables in FP64 arithmetic (the
+// split form with FP64 kept for the state arithmetic), else in float-float;
+// the flux divergence is formed in FP32 and the CT curl in FP64 in both.
+// rd: (ra, rb) and (dt/dx, dt/dy, dt/dz) times the stencil's 1/24, as
+// doubles.
 struct RkF64 {
     double ra, rb, ddx, ddy, ddz;
 };
@@ -703,7 +736,7 @@ struct RkF64 {
 template <bool F64>
 __global__ void __launch_bounds__(128)
 ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, RkF64 rd, float dtdx, float dtdy,
-          float dtdz, float2 ddx2, float2 ddy2, float2 ddz2, int k0)
+          float dtdz, int images, int k0)
 {
     const int i = d.ox + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = d.oy + blockIdx.y, k = k0 + blockIdx.z;
@@ -732,44 +765,36 @@ ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, RkF64 rd, float 
         u[v] = f.s[v][s];
         u0[v] = rk.first ? 0.0 : __ldg(f.u0[v] + s);
     }
-    // arithmetic
+    // arithmetic: the flux divergence of the cell-centred variables
     double out[8];
-    if constexpr (F64) {
 #pragma unroll
-        for (int v = 0; v < 5; v++) {
-            const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
-                              + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
-                              + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
+    for (int v = 0; v < 5; v++) {
+        const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
+                          + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
+                          + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
+        if constexpr (F64) {
             const double w = u[v] - to_f64(div);
             out[v] = rk.first ? w : rd.ra * u0[v] + rd.rb * w;
-        }
-        const double b5 = u[5] - rd.ddy * df_f64(odr, ezy) + rd.ddz * df_f64(odr, eyz);
-        const double b6 = u[6] - rd.ddz * df_f64(odr, exz) + rd.ddx * df_f64(odr, ezx);
-        const double b7 = u[7] - rd.ddx * df_f64(odr, eyx) + rd.ddy * df_f64(odr, exy);
-        out[5] = rk.first ? b5 : rd.ra * u0[5] + rd.rb * b5;
-        out[6] = rk.first ? b6 : rd.ra * u0[6] + rd.rb * b6;
-        out[7] = rk.first ? b7 : rd.ra * u0[7] + rd.rb * b7;
-    } else {
-#pragma unroll
-        for (int v = 0; v < 5; v++) {
-            const float div = dtdx * fdiff(odr, fx[v][0], fx[v][1], fx[v][2], fx[v][3])
-                              + dtdy * fdiff(odr, fy[v][0], fy[v][1], fy[v][2], fy[v][3])
-                              + dtdz * fdiff(odr, fz[v][0], fz[v][1], fz[v][2], fz[v][3]);
+        } else {
             // the first stage is u - div: one FP64 addition beats its float-float form
             out[v] = rk.first ? u[v] - to_f64(div)
                               : rk_ff(rk, u0[v], ff_add_f(ff_from(u[v]), -div));
         }
-        // CT curl in float-float: the differences of the FP32 edge EMFs are
-        // exact, so the discrete divergence of the B increment cancels to the
-        // float-float round-off (in FP32, 27*(E2-E1) alone would need more than
-        // 24 bits).  ddx2 etc. carry the stencil's 1/24 when odr > 2.
-        const ff ddx = {ddx2.x, ddx2.y}, ddy = {ddy2.x, ddy2.y}, ddz = {ddz2.x, ddz2.y};
-        out[5] = rk_ff(rk, u0[5], ff_add(ff_sub(ff_from(u[5]), ff_mul(ddy, df_ff(odr, ezy))),
-                                         ff_mul(ddz, df_ff(odr, eyz))));
-        out[6] = rk_ff(rk, u0[6], ff_add(ff_sub(ff_from(u[6]), ff_mul(ddz, df_ff(odr, exz))),
-                                         ff_mul(ddx, df_ff(odr, ezx))));
-        out[7] = rk_ff(rk, u0[7], ff_add(ff_sub(ff_from(u[7]), ff_mul(ddx, df_ff(odr, eyx))),
-                                         ff_mul(ddy, df_ff(odr, exy))));
+    }
+    // CT curl of face B in FP64 in both forms: the EMF differences of the
+    // converted FP32 values and their products with dt/dx are rounded to 53
+    // bits, so the discrete divergence of the B increment cancels to FP64
+    // round-off (float-float, 48 bits, let it grow some 30 times faster).
+    const double b5 = u[5] - rd.ddy * df_f64(odr, ezy) + rd.ddz * df_f64(odr, eyz);
+    const double b6 = u[6] - rd.ddz * df_f64(odr, exz) + rd.ddx * df_f64(odr, ezx);
+    const double b7 = u[7] - rd.ddx * df_f64(odr, eyx) + rd.ddy * df_f64(odr, exy);
+    out[5] = rk.first ? b5 : rd.ra * u0[5] + rd.rb * b5;
+    out[6] = rk.first ? b6 : rd.ra * u0[6] + rd.rb * b6;
+    out[7] = rk.first ? b7 : rd.ra * u0[7] + rd.rb * b7;
+    if (!images) {  // non-periodic tables: the ghost fill follows
+#pragma unroll
+        for (int v = 0; v < 8; v++) f.s[v][s] = out[v];
+        return;
     }
     const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
     const int is[3] = {i, i < 2 * d.ox ? i + Nx : -1, i >= Nx ? i - Nx : -1};
@@ -786,6 +811,46 @@ ks_update(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, RkF64 rd, float 
                 for (int v = 0; v < 8; v++) f.s[v][t] = out[v];
             }
         }
+    }
+}
+
+// The right boundary faces the reference's CT loops also update (Bx at
+// i = nx-xoff, By at j = ny-yoff, Bz at k = nz-zoff; mhd_fd_ct_3d.c:1079-1157
+// run one face further); with non-periodic tables they survive the ghost fill
+// where that axis mirrors the face array.  Same FP64 curl as ks_update, one
+// thread per face of the three planes.
+__global__ void __launch_bounds__(128)
+ks_face(PlainFields f, SplitPtrs g, Dims d, int odr, RkFF rk, RkF64 rd, int do_x, int do_y,
+        int do_z)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long sy = d.px, sz = d.px * d.ny;  // scratch strides
+    const int Nx = d.nx - 2 * d.ox, Ny = d.ny - 2 * d.oy, Nz = d.nz - 2 * d.oz;
+    auto put = [&](int v, int i, int j, int k, double b) {
+        const long long s = d.at(i, j, k);
+        f.s[v][s] = rk.first ? b : rd.ra * f.u0[v][s] + rd.rb * b;
+    };
+    float e0[4], e1[4];
+    if (do_x && t < (long long)Ny * Nz) {  // Bx at i = nx - xoff
+        const int i = d.nx - d.ox, j = d.oy + (int)(t % Ny), k = d.oz + (int)(t / Ny);
+        const long long sp = d.ap(i, j, k);
+        ld4(e0, g.e[2], sp, sy);
+        ld4(e1, g.e[1], sp, sz);
+        put(5, i, j, k, f.s[5][d.at(i, j, k)] - rd.ddy * df_f64(odr, e0) + rd.ddz * df_f64(odr, e1));
+    }
+    if (do_y && t < (long long)Nx * Nz) {  // By at j = ny - yoff
+        const int i = d.ox + (int)(t % Nx), j = d.ny - d.oy, k = d.oz + (int)(t / Nx);
+        const long long sp = d.ap(i, j, k);
+        ld4(e0, g.e[0], sp, sz);
+        ld4(e1, g.e[2], sp, 1);
+        put(6, i, j, k, f.s[6][d.at(i, j, k)] - rd.ddz * df_f64(odr, e0) + rd.ddx * df_f64(odr, e1));
+    }
+    if (do_z && t < (long long)Nx * Ny) {  // Bz at k = nz - zoff
+        const int i = d.ox + (int)(t % Nx), j = d.oy + (int)(t / Nx), k = d.nz - d.oz;
+        const long long sp = d.ap(i, j, k);
+        ld4(e0, g.e[1], sp, 1);
+        ld4(e1, g.e[0], sp, sy);
+        put(7, i, j, k, f.s[7][d.at(i, j, k)] - rd.ddx * df_f64(odr, e0) + rd.ddy * df_f64(odr, e1));
     }
 }
 
@@ -1009,12 +1074,18 @@ struct StepCtx {
     // primitive recovery of planes [k0, k0 + nk)
     void prim(int rk, int k0, int nk) const
     {
-        auto kern = s->sp->f64 ? ks_prim<true> : ks_prim<false>;
-        kern<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->f, s->sp->p, d, s->odr,
+        const bool w = s->walls3d;
+        auto kern = s->sp->f64 ? (w ? ks_prim<true, true> : ks_prim<true, false>)
+                               : (w ? ks_prim<false, true> : ks_prim<false, false>);
+        kern<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->f, s->sp->p, d, s->bc3, s->odr,
                                                    host_ff(s->gamma - 1), s->gamma - 1,
                                                    (float)s->gamma, rk == 0, k0);
     }
-    void aux() const { ks_aux<<<cg, cb, 0, s->stream>>>(s->sp->p, d); }
+    void aux() const
+    {
+        auto kern = s->walls3d ? ks_aux<true> : ks_aux<false>;
+        kern<<<cg, cb, 0, s->stream>>>(s->sp->p, d, s->bc3);
+    }
     void sweeps() const
     {
         const float gam = (float)s->gamma;
@@ -1037,8 +1108,17 @@ struct StepCtx {
         auto kern = s->sp->f64 ? ks_update<true> : ks_update<false>;
         kern<<<dim3(ug.x, ug.y, nk), cb, 0, s->stream>>>(
             s->f, s->sp->p, d, s->odr, c, c64, (float)(dt / G.dx), (float)(dt / G.dy),
-            (float)(dt / G.dz), host_ff(dt / G.dx * c24), host_ff(dt / G.dy * c24),
-            host_ff(dt / G.dz * c24), k0);
+            (float)(dt / G.dz), !s->walls3d, k0);
+        if (s->walls3d && k0 + nk == G.nz - G.oz) {
+            // after the last interior plane: the right boundary faces, then
+            // the ghost fill with the tables
+            const long long n = std::max({(long long)G.ny * G.nz, (long long)G.nx * G.nz,
+                                          (long long)G.nx * G.ny});
+            ks_face<<<blocks_for(n, 128), 128, 0, s->stream>>>(
+                s->f, s->sp->p, d, s->odr, c, c64, s->bc3.x[5] != 0, s->bc3.y[6] != 0,
+                s->bc3.z[7] != 0);
+            plain3d_fill_ghosts(s);
+        }
     }
 };
 
