@@ -318,7 +318,7 @@ __device__ void ph_update(const BArgs &A, int nt, const BTile *tl, int rk)
 }
 
 // One full RK3 step of every active instance.
-__global__ void __launch_bounds__(256) kb_step_split(BArgs A)
+__global__ void __launch_bounds__(256, 3) kb_step_split(BArgs A)
 {
     const int nt = A.sync->ntiles;
     const BTile *tl = A.sync->tiles;

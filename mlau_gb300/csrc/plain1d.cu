@@ -32,15 +32,58 @@ __global__ void k_prim1(PlainFields f, int nx, double bx, double gamma, int save
 }
 
 // Face states (:133-186): full characteristic system where any of the three
-// central cells has sonic Mach^2 >= 1.
+// central cells has sonic Mach^2 >= 1, Alfven + entropy system elsewhere.
+//
+// A cell's work is spread over 8 lanes: on this part a warp's FP64
+// instruction holds its sub-partition's FP64 pipe for 64 cycles, and a
+// 2048-cell grid at one cell per thread is 64 warps running one long serial
+// chain each.  Lane r (0..6) projects the stencil on characteristic field r,
+// interpolates it and back-projects output r; lane 7 repeats field 6 and
+// stores nothing.  Every lane evaluates the cell's eigen-system (the same
+// values).  The projections and back-projections are the dense 7-term sums of
+// include/mhd_eigen.h (:455-684) in its order, the same on every lane (no
+// divergence), so the face values equal those of the one-lane form and the
+// reference's; the lanes exchange the interpolated fields by warp shuffles.
+constexpr int RLANES = 8;
+
+// Left eigenvector n (Ln[k] = L[n][k]) and entry n of every right
+// eigenvector (Rc[k] = R[k][n], the back-projection's coefficients of output
+// n) from a dense fill, selected with unrolled predicated moves so that the
+// 7x7 matrices stay in registers and their constant entries fold away;
+// eigenvalue n into *lam.
+template <class FILL>
+__device__ __forceinline__ void eig_row(FILL fill, int n, double Ln[7], double Rc[7], double *lam)
+{
+    double al[7], L[7][7], R[7][7];
+    fill(al, L, R);
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        Ln[k] = L[0][k];
+        Rc[k] = R[k][0];
+    }
+    *lam = al[0];
+#pragma unroll
+    for (int j = 1; j < 7; j++) {
+#pragma unroll
+        for (int k = 0; k < 7; k++) {
+            Ln[k] = (n == j) ? L[j][k] : Ln[k];
+            Rc[k] = (n == j) ? R[k][j] : Rc[k];
+        }
+        *lam = (n == j) ? al[j] : *lam;
+    }
+}
+
 __global__ void k_rec1(PlainFields f, int nx, int odr, int eig, double bx, double gamma)
 {
-    const int i = 2 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nx - 2) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = t & (RLANES - 1), i = 2 + t / RLANES;
+    const bool live = i < nx - 2;
+    const int ic = live ? i : nx - 3;  // every lane takes part in the shuffles
+    const int n = r < 7 ? r : 6;
     double q[7][5];
 #pragma unroll
     for (int m = 0; m < 5; m++) {
-        const int s = i + m - 2;
+        const int s = ic + m - 2;
         q[0][m] = f.s[0][s];
         q[1][m] = f.vx[s];
         q[2][m] = f.vy[s];
@@ -51,18 +94,64 @@ __global__ void k_rec1(PlainFields f, int nx, int odr, int eig, double bx, doubl
     }
     double mach[3];
 #pragma unroll
-    for (int t = 0; t < 3; t++) {
-        const double c2 = gamma * q[6][1 + t] / q[0][1 + t];
-        const double v2 = q[1][1 + t] * q[1][1 + t] + q[2][1 + t] * q[2][1 + t]
-                          + q[3][1 + t] * q[3][1 + t];
-        mach[t] = v2 / c2;
+    for (int u = 0; u < 3; u++) {
+        const double c2 = gamma * q[6][1 + u] / q[0][1 + u];
+        const double v2 = q[1][1 + u] * q[1][1 + u] + q[2][1 + u] * q[2][1 + u]
+                          + q[3][1 + u] * q[3][1 + u];
+        mach[u] = v2 / c2;
     }
-    double ul[7], ur[7];
-    reconst_face(odr, eig, vmax(mach[0], vmax(mach[1], mach[2])), q, bx, gamma, ul, ur);
+    // Ln: the lane's left eigenvector; Rc[j]: entry n of right eigenvector j
+    // (the back-projection's coefficient of field j in output n)
+    double Ln[7], Rc[7], lam;
+    const double c0 = q[0][2], c1 = q[1][2], c2 = q[2][2], c3 = q[3][2], c4 = q[4][2],
+                 c5 = q[5][2], c6 = q[6][2];
+    if (vmax(mach[0], vmax(mach[1], mach[2])) >= 1.0) {
+        if (eig == EIG_MIYOSHI)
+            eig_row([&](double *a, double (*L)[7], double (*R)[7]) {
+                eigen_mi_dense(c0, c1, c2, c3, bx, c4, c5, c6, gamma, a, L, R); }, n, Ln, Rc, &lam);
+        else
+            eig_row([&](double *a, double (*L)[7], double (*R)[7]) {
+                eigen_st_dense(c0, c1, c2, c3, bx, c4, c5, c6, gamma, a, L, R); }, n, Ln, Rc, &lam);
+    } else {
+        eig_row([&](double *a, double (*L)[7], double (*R)[7]) {
+            eigen_ae_dense(c0, c1, c2, c3, bx, c4, c5, c6, gamma, a, L, R); }, n, Ln, Rc, &lam);
+    }
+    double w[5];
 #pragma unroll
-    for (int n = 0; n < 7; n++) {
-        f.ul[n][i + 1] = ul[n];
-        f.ur[n][i] = ur[n];
+    for (int m = 0; m < 5; m++)
+        w[m] = (+Ln[0] * q[0][m] + Ln[1] * q[1][m] + Ln[2] * q[2][m] + Ln[3] * q[3][m]
+                + Ln[4] * q[4][m] + Ln[5] * q[5][m] + Ln[6] * q[6][m]);
+    double wl, wr;
+    rec_lr(odr, w, wl, wr);
+    // blocks of fewer than 32 threads are one partial warp
+    const unsigned mask = blockDim.x >= 32 ? 0xffffffffu : (1u << blockDim.x) - 1u;
+    const int g0 = (threadIdx.x & 31) & ~(RLANES - 1);
+    double fl[7], fr[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        fl[k] = __shfl_sync(mask, wl, g0 + k);
+        fr[k] = __shfl_sync(mask, wr, g0 + k);
+    }
+    double ul = Rc[0] * fl[0] + Rc[1] * fl[1] + Rc[2] * fl[2] + Rc[3] * fl[3] + Rc[4] * fl[4]
+                + Rc[5] * fl[5] + Rc[6] * fl[6];
+    double ur = Rc[0] * fr[0] + Rc[1] * fr[1] + Rc[2] * fr[2] + Rc[3] * fr[3] + Rc[4] * fr[4]
+                + Rc[5] * fr[5] + Rc[6] * fr[6];
+    // exact-zero guard (mhd_eigen.h:516-529): output n of a field that is zero
+    // across the stencil
+    bool zero = false;
+#pragma unroll
+    for (int k = 1; k <= 5; k++) {
+        const bool z = q[k][0] == 0.0 && q[k][1] == 0.0 && q[k][2] == 0.0 && q[k][3] == 0.0 &&
+                       q[k][4] == 0.0;
+        zero = (n == k) ? z : zero;
+    }
+    if (zero) {
+        ul = 0.0;
+        ur = 0.0;
+    }
+    if (live && r < 7) {
+        f.ul[n][i + 1] = ul;
+        f.ur[n][i] = ur;
     }
 }
 
@@ -83,69 +172,78 @@ __global__ void k_flux1(PlainFields f, int nx, int which, double bx, double gamm
 
 // openbc1d_mhd (1D/SERIAL/shock/openbc1d_mhd.c:21-175).  The two sides read
 // and write disjoint cells (interior width >= ghost depth), so each runs in
-// its own block: block 0 the left side, block 1 the right.
+// its own block of 8 lanes: block 0 the left side, block 1 the right.  Lane r
+// (0..6) projects both cells on characteristic field r and applies its
+// outflow condition; the back-projection of primitive r follows the dense
+// 7-term sums of the header, with the fields exchanged by shuffles; lane 0
+// converts to conserved variables and fills the ghost cells.
 __global__ void k_openbc1(PlainFields f, int nx, int xoff, double bx, double dtdx, double gamma)
 {
-    if (threadIdx.x != 0 || blockIdx.x > 1) return;
+    const int r = threadIdx.x;
+    if (blockIdx.x > 1 || r >= 8) return;  // launched with 8 threads per block
+    const int n = r < 7 ? r : 6;
     double *ro = f.s[0], *mx = f.s[1], *my = f.s[2], *mz = f.s[3], *en = f.s[4], *by = f.s[6],
            *bz = f.s[7];
     const double bx2 = bx * bx;
-    {
-        const int side = blockIdx.x;
-        const int sgn = side ? -1 : 1;
-        const int si = side ? (nx - xoff - 1) : xoff;
-        const int so = si - sgn;
-        double q[2][7];
-        for (int t = 0; t < 2; t++) {
-            const int s = t ? so : si;
-            const double r = ro[s], iro = 1.0 / r;
-            const double vx = mx[s] * iro, vy = my[s] * iro, vz = mz[s] * iro;
-            const double v2 = vx * vx + vy * vy + vz * vz;
-            const double b2 = bx * bx + by[s] * by[s] + bz[s] * bz[s];
-            q[t][0] = r;
-            q[t][1] = vx;
-            q[t][2] = vy;
-            q[t][3] = vz;
-            q[t][4] = by[s];
-            q[t][5] = bz[s];
-            q[t][6] = (gamma - 1) * (en[s] - 0.5 * (r * v2 + b2));
-        }
-        Eigen7<double> E;
-        eigen_full(0.5 * (q[0][0] + q[1][0]), 0.5 * (q[0][1] + q[1][1]), 0.5 * (bx + bx),
-                   0.5 * (q[0][4] + q[1][4]), 0.5 * (q[0][5] + q[1][5]), 0.5 * (q[0][6] + q[1][6]),
-                   gamma, E);
-        double w0[7], w1[7];
-        proj_full(E, q[0][0], q[0][1], q[0][2], q[0][3], q[0][4], q[0][5], q[0][6], w0);
-        proj_full(E, q[1][0], q[1][1], q[1][2], q[1][3], q[1][4], q[1][5], q[1][6], w1);
-        for (int m = 0; m < 7; m++) {
-            const double c = sgn * E.lam[m];
-            w1[m] = (c > 0) ? w1[m] : (1 + c * dtdx) * w1[m] - c * dtdx * w0[m];
-        }
-        double p[7];
-        back_full(E, w1, p);
-        ro[so] = p[0];
-        mx[so] = p[1];
-        my[so] = p[2];
-        mz[so] = p[3];
-        by[so] = p[4];
-        bz[so] = p[5];
-        en[so] = p[6];
-        const double v2 = mx[so] * mx[so] + my[so] * my[so] + mz[so] * mz[so];
-        const double b2 = bx2 + by[so] * by[so] + bz[so] * bz[so];
-        en[so] = en[so] / (gamma - 1.0) + 0.5 * (ro[so] * v2 + b2);
-        mx[so] *= ro[so];
-        my[so] *= ro[so];
-        mz[so] *= ro[so];
-        for (int j = 0; j < xoff - 1; j++) {
-            const int s = side * (nx - 1) + sgn * j;
-            ro[s] = ro[so];
-            mx[s] = mx[so];
-            my[s] = my[so];
-            mz[s] = mz[so];
-            by[s] = by[so];
-            bz[s] = bz[so];
-            en[s] = en[so];
-        }
+    const int side = blockIdx.x;
+    const int sgn = side ? -1 : 1;
+    const int si = side ? (nx - xoff - 1) : xoff;
+    const int so = si - sgn;
+    double q[2][7];
+    for (int t = 0; t < 2; t++) {
+        const int s = t ? so : si;
+        const double rr = ro[s], iro = 1.0 / rr;
+        const double vx = mx[s] * iro, vy = my[s] * iro, vz = mz[s] * iro;
+        const double v2 = vx * vx + vy * vy + vz * vz;
+        const double b2 = bx * bx + by[s] * by[s] + bz[s] * bz[s];
+        q[t][0] = rr;
+        q[t][1] = vx;
+        q[t][2] = vy;
+        q[t][3] = vz;
+        q[t][4] = by[s];
+        q[t][5] = bz[s];
+        q[t][6] = (gamma - 1) * (en[s] - 0.5 * (rr * v2 + b2));
+    }
+    double Ln[7], Rc[7], lam;
+    eig_row([&](double *a, double (*L)[7], double (*R)[7]) {
+        eigen_st_dense(0.5 * (q[0][0] + q[1][0]), 0.5 * (q[0][1] + q[1][1]), 0.0, 0.0,
+                       0.5 * (bx + bx), 0.5 * (q[0][4] + q[1][4]), 0.5 * (q[0][5] + q[1][5]),
+                       0.5 * (q[0][6] + q[1][6]), gamma, a, L, R); }, n, Ln, Rc, &lam);
+    double w[2];
+    for (int t = 0; t < 2; t++)
+        w[t] = (+Ln[0] * q[t][0] + Ln[1] * q[t][1] + Ln[2] * q[t][2] + Ln[3] * q[t][3]
+                + Ln[4] * q[t][4] + Ln[5] * q[t][5] + Ln[6] * q[t][6]);
+    const double c = sgn * lam;
+    const double w1 = (c > 0) ? w[1] : (1 + c * dtdx) * w[1] - c * dtdx * w[0];
+    double wv[7];
+    for (int k = 0; k < 7; k++) wv[k] = __shfl_sync(0xffu, w1, k, 8);
+    const double pn = Rc[0] * wv[0] + Rc[1] * wv[1] + Rc[2] * wv[2] + Rc[3] * wv[3]
+                      + Rc[4] * wv[4] + Rc[5] * wv[5] + Rc[6] * wv[6];
+    double p[7];
+    for (int k = 0; k < 7; k++) p[k] = __shfl_sync(0xffu, pn, k, 8);
+    if (r != 0) return;
+    ro[so] = p[0];
+    mx[so] = p[1];
+    my[so] = p[2];
+    mz[so] = p[3];
+    by[so] = p[4];
+    bz[so] = p[5];
+    en[so] = p[6];
+    const double v2 = mx[so] * mx[so] + my[so] * my[so] + mz[so] * mz[so];
+    const double b2 = bx2 + by[so] * by[so] + bz[so] * bz[so];
+    en[so] = en[so] / (gamma - 1.0) + 0.5 * (ro[so] * v2 + b2);
+    mx[so] *= ro[so];
+    my[so] *= ro[so];
+    mz[so] *= ro[so];
+    for (int j = 0; j < xoff - 1; j++) {
+        const int s = side * (nx - 1) + sgn * j;
+        ro[s] = ro[so];
+        mx[s] = mx[so];
+        my[s] = my[so];
+        mz[s] = mz[so];
+        by[s] = by[so];
+        bz[s] = bz[so];
+        en[s] = en[so];
     }
 }
 
@@ -190,8 +288,9 @@ int plain1d_alloc(Sim *s)
 
 // 1D grids hold a few thousand cells, each cell a long chain of FP64
 // operations: blocks of 32 threads spread a 2048-cell problem over 64 SMs
-// instead of 16 (0.208 instead of 0.222 ms per step at 2048 cells; the rest
-// is each warp's own FP64 chain and the launches).
+// instead of 16 at 128 threads.  Smaller blocks measured slower (16: 0.181,
+// 8: 0.282 ms per step against 0.151): a partial warp's FP64 instruction
+// holds the pipe as long as a full one.
 constexpr int T1D = 32;
 
 int plain1d_step(Sim *s, double dt)
@@ -211,7 +310,8 @@ int plain1d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_REC);
-            k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, s->odr, s->eig, s->bx1d, s->gamma);
+            k_rec1<<<blocks_for((long long)(nx - 4) * RLANES, T), T, 0, st>>>(f, nx, s->odr, s->eig,
+                                                                            s->bx1d, s->gamma);
         }
         {
             TimedLaunch tl(&s->timer, KK_FLUX);
@@ -219,7 +319,7 @@ int plain1d_step(Sim *s, double dt)
         }
         if (s->bc1d == MLAU_BC1D_OPEN && rk == 0) {
             TimedLaunch tl(&s->timer, KK_AUX);
-            k_openbc1<<<2, 1, 0, st>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
+            k_openbc1<<<2, 8, 0, st>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
         }
         {
             TimedLaunch tl(&s->timer, KK_UPDATE);
@@ -247,9 +347,10 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
         double ra, rb;
         rk_coef(nrk, rk, ra, rb);
         k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma, rk == 0);
-        k_rec1<<<blocks_for(nx - 4, T), T, 0, st>>>(f, nx, odr, EIG_FULL, bx, gamma);
+        k_rec1<<<blocks_for((long long)(nx - 4) * RLANES, T), T, 0, st>>>(f, nx, odr, EIG_FULL,
+                                                                        bx, gamma);
         k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
-        if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<2, 1, 0, st>>>(f, nx, off, bx, dtdx, gamma);
+        if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<2, 8, 0, st>>>(f, nx, off, bx, dtdx, gamma);
         k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(f, nx, off, odr, ra, rb, dtdx,
                                                             bc == MLAU_BC1D_PERIODIC);
         MLAU_CUDA(cudaGetLastError());

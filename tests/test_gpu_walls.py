@@ -200,9 +200,16 @@ def test_walls_3d_split_vs_fp64(prec, tables, odr, flux):
     """Both FP32-split forms with Dirichlet / Neumann mirrors (cell B and the
     shock sensors at their signed sources, the right boundary faces, the ghost
     fill of the FP64 state) against the FP64 step with the same tables:
-    relative L1 of density and energy <= 1e-6 over every cell, ghosts
-    included (a ghost filled from the wrong source would differ at O(1)), and
-    the interior div B kept at round-off from the first step on."""
+    relative L1 over every cell, ghosts included (a ghost filled from the
+    wrong source, or a wrong boundary face, would differ at O(1) there),
+    <= 1e-6 for density and energy and <= 1e-5 for face B.  div B, from the
+    first step on: at round-off (1e-12) in cells two or more cells away from a
+    mirror wall; next to a wall the ghost faces are mirror copies, and the
+    FP32 EMFs there are mirror-symmetric only to FP32 rounding, so div B
+    drifts at that level (bound 1e-9 after 19 steps; the FP64 step keeps
+    2e-15).  The all-Neumann tables are left out of the div B check: they
+    mirror face B with the wrong parity, and the reference's own step does not
+    keep div B with them (4.7e-3 after 19 steps on this state)."""
     st, m = ics.turbulence_3d(n=16, ny=12, nz=10, mach=0.3, seed=odr * 5 + len(flux), odr=odr)
     dt = 0.3 * m["dx"] / m["vfast"]
     out = {}
@@ -216,11 +223,31 @@ def test_walls_3d_split_vs_fp64(prec, tables, odr, flux):
             s.step(dt, 19)
             out[p] = (first, s.download())
     (f0, ref), (f1, got) = out[M.FP64], out[prec]
-    for k in ("ro", "en"):
+    for k, tol in (("ro", 1e-6), ("en", 1e-6), ("bx", 1e-5), ("by", 1e-5), ("bz", 1e-5)):
         assert np.isfinite(got[k]).all(), k
         l1 = np.abs(got[k] - ref[k]).sum() / np.abs(ref[k]).sum()
-        assert l1 <= 1e-6, (k, l1)
-    assert ics.div_b_3d(got, m["dx"], m["dy"], m["dz"], odr=odr, base=f1) <= 1e-12
+        assert l1 <= tol, (k, l1)
+    if tables == TABLES_3D[4]:
+        return
+    walls = [any(t) for t in tables]  # x, y, z axes with mirrors
+    margin = tuple(6 if w else 4 for w in walls[::-1])  # (z, y, x) cells cut from each end
+    assert div_b_change(got, f1, m, odr, margin) <= 1e-12
+    assert div_b_change(got, f1, m, odr, (4, 4, 4)) <= 1e-9
+
+
+def div_b_change(st, base, m, odr, margin):
+    """max |div B - div B(base)| * dx / max |B| over the cells `margin` cells
+    away from each end of every axis (z, y, x), with the scheme's difference."""
+    def d(f, ax, h):
+        f2 = np.roll(f, -1, axis=ax)
+        if odr <= 2 or odr > 4:
+            return (f2 - f) / h
+        return (27.0 * (f2 - f) - (np.roll(f, -2, axis=ax) - np.roll(f, 1, axis=ax))) / 24.0 / h
+    def div(s):
+        return d(s["bx"], 2, m["dx"]) + d(s["by"], 1, m["dy"]) + d(s["bz"], 0, m["dz"])
+    sl = tuple(slice(a, -a) for a in margin)
+    bmax = max(np.abs(st[k][(slice(4, -4),) * 3]).max() for k in ("bx", "by", "bz"))
+    return float(np.abs((div(st) - div(base))[sl]).max() * min(m["dx"], m["dy"], m["dz"]) / bmax)
 
 
 @pytest.mark.parametrize("prec", (M.FP32_SPLIT, M.FP32_SPLIT_F64))
