@@ -518,6 +518,7 @@ def run_step1d(args):
     gamma=2, CFL 0.4, open boundaries, dt fixed from the initial state, run to
     t_end=0.1 as the 1D driver does; the whole run is timed (one problem is
     launch-latency bound: 13 launches per step)."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     import mlau_gb300 as M
     from mlau_gb300 import ics
     from oracle import Port
@@ -549,10 +550,13 @@ def run_step1d(args):
             "config": {"workload": "1D Riemann problem, 2048 cells, MLAU + MUSCL-minmod + RK3, "
                                    "gamma=2, CFL 0.4, open boundaries, t_end 0.1",
                        "time_to_solution_ms": ms, "l2": "fits in L2 (one resident problem)"},
-            "roofline": None, "roofline_note": "latency bound: 13 launches of ~2k threads per step",
+            "roofline": None,
+            "roofline_note": "latency bound: each warp's FP64 chain (a warp FP64 instruction holds "
+                             "its sub-partition's pipe 64 cycles) and 13 launches per step",
             "gpu_launches": launches, "clocks": clk.summary(),
-            "cpu_baseline": {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"the whole run, {nsteps} steps"}}
+            "cpu_baseline": {"value": cv, "unit": UNIT,
+                             "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                             "sample": f"the whole run, {nsteps} steps, OpenMP"}}
 
 
 # --- batched 2D and serving workloads ------------------------------------------
@@ -671,6 +675,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end drop-in measurement (profiling runs)")
+    ap.add_argument("--no-config-samples", dest="config_samples", action="store_false",
+                    help="skip the 1D / 2D / MRX samples of the default line")
     ap.add_argument("--batch-sample", type=int, default=64,
                     help="instances of the batched-engine sample in the default line (0: skip)")
     ap.add_argument("--accuracy-steps", type=int, default=200,
@@ -781,6 +787,19 @@ def main():
             bl = run_batch2d(args, n_inst=args.batch_sample, steps=5, warmup=3)
             line["batch2d_sample"] = {k: bl[k] for k in ("metric", "value", "unit", "ms_per_step",
                                                          "steps", "config", "clocks")}
+        if args.config_samples and R.world == 1 and args.precision == "both":
+            # bounded samples of the other configurations, so that the default
+            # run records them too: 1D Riemann problem to t_end, 2D 512^2, the
+            # MRX loop (each with its CPU restatement beside it)
+            a2 = argparse.Namespace(**vars(args))
+            a2.steps, a2.warmup, a2.cpu_steps = 20, 3, 1
+            samples = {}
+            for name, fn in (("step1d", run_step1d), ("step2d", run_step2d), ("mrx2d", run_mrx2d)):
+                r2 = fn(a2)
+                samples[name] = {k: r2.get(k) for k in ("metric", "value", "unit", "ms_per_step",
+                                                        "steps", "config", "cpu_baseline",
+                                                        "roofline")}
+            line["config_samples"] = samples
         if args.accuracy_steps > 0 and R.world == 1 and args.precision == "both":
             # the configuration's 200-step accuracy record at both Mach numbers
             line["accuracy"] = [run_accuracy(args.n, mach, args.accuracy_steps)

@@ -267,14 +267,15 @@ int mlau_outdat_meta(const char *dir, int dim, int first, double tim, double gam
 /* ---------------------------------------------------------------------- */
 /* 5. Batched 2D engine                                                    */
 /* ---------------------------------------------------------------------- */
-/* Many independent periodic 2D instances (the 2D driver's scheme,
+/* Many independent 2D instances (the 2D driver's scheme,
  * 2D/SERIAL/OTvortex/mhd_fd_ct_2d.c, RK3) in slots of one engine, each with
  * its own grid size (nx, ny padded), cell sizes, gamma, Riemann solver, CFL
  * number and end time.  One persistent cooperative kernel per step walks a
  * per-instance tile table; each instance takes its own CFL dt every step
  * (clipped to land on its end time) and retires when it gets there.
+ * Instances are periodic unless mlau_batch_set_bc gives them tables.
  * Precision per engine: MLAU_FP64 (each instance bit-identical to
- * mhd_fd_ct_2d) or MLAU_FP32_SPLIT.  Instances join and leave between runs
+ * mhd_fd_ct_2d, with its boundary tables) or MLAU_FP32_SPLIT.  Instances join and leave between runs
  * (continuous batching).  No reference counterpart (the reference runs one
  * problem per process). */
 typedef struct mlau_batch mlau_batch;
@@ -296,6 +297,12 @@ int mlau_batch_upload(mlau_batch *b, int inst, const double *const *host8);
 int mlau_batch_download(mlau_batch *b, int inst, double *const *host8);
 /* dt > 0: fixed time step for that instance instead of its CFL step. */
 int mlau_batch_set_fixed_dt(mlau_batch *b, int inst, double dt);
+/* Boundary tables of a 2D instance - the problem's dnxs / dnys
+ * (2D/SERIAL/OTvortex/global.hpp:22-29, 0 periodic, -1 Dirichlet, +1 Neumann
+ * per variable ro mx my mz en bx by bz), applied as mhd_fd_ct_2d applies
+ * them (bc2d, 2D/SERIAL/OTvortex/boundary.c:18-74); all zero (the default) is
+ * periodic.  Set between runs, before the instance's next step. */
+int mlau_batch_set_bc(mlau_batch *b, int inst, const int *dnx, const int *dny);
 /* Tile shape TW x TH (= 256 threads, TW a multiple of 16). */
 int mlau_batch_set_tile(mlau_batch *b, int tw, int th);
 /* Grid of the persistent step kernel: nblocks co-resident blocks (clamped to

@@ -90,6 +90,7 @@ def _bind(lib):
     lib.mlau_batch_upload.argtypes = [vp, i, C.POINTER(pd)]
     lib.mlau_batch_download.argtypes = [vp, i, C.POINTER(pd)]
     lib.mlau_batch_set_fixed_dt.argtypes = [vp, i, d]
+    lib.mlau_batch_set_bc.argtypes = [vp, i, C.POINTER(i), C.POINTER(i)]
     lib.mlau_batch_set_tile.argtypes = [vp, i, i]
     lib.mlau_batch_autotune.argtypes = [vp, i, pi, pi, pd]
     lib.mlau_batch_run.argtypes = [vp, i, i, pi, pd]
@@ -572,6 +573,11 @@ class Batch:
 
     def set_fixed_dt(self, k, dt):
         _check(lib().mlau_batch_set_fixed_dt(self._h, k, dt))
+
+    def set_bc(self, k, dnx, dny):
+        """Boundary tables (the problem's dnxs, dnys) of 2D instance k."""
+        tab = lambda t: (C.c_int * 8)(*[int(x) for x in t])
+        _check(lib().mlau_batch_set_bc(self._h, k, tab(dnx), tab(dny)))
 
     def set_tile(self, tw, th):
         _check(lib().mlau_batch_set_tile(self._h, tw, th))

@@ -189,6 +189,7 @@ int push_table(mlau_batch *b)
         if (!b->used[n] || !I.active) continue;
         s0.active_left++;
         if (b->dim == 1 && I.steps == 0 && !(I.dt_fixed > 0.0)) s0.fresh = 1;
+        if (b->dim == 2 && I.walls) s0.walls = 1;
     }
     s0.ntiles = b->ntiles;
     s0.tiles = b->d_tiles;
@@ -531,6 +532,30 @@ int mlau_batch_download(mlau_batch *b, int n, double *const *h)
             MLAU_CUDA(cudaMemcpyAsync(h[v], b->a.s[v] + I.base, bytes, cudaMemcpyDeviceToHost,
                                       b->stream));
     MLAU_CUDA(cudaStreamSynchronize(b->stream));
+    return MLAU_OK;
+}
+
+int mlau_batch_set_bc(mlau_batch *b, int n, const int *dnx, const int *dny)
+{
+    if (!check_inst(b, n)) return MLAU_ERR_ARG;
+    if (b->dim != 2 || !dnx || !dny) {
+        set_error("batch: boundary tables apply to 2D instances");
+        return MLAU_ERR_ARG;
+    }
+    BInst &I = b->h_inst[n];
+    int walls = 0;
+    for (int v = 0; v < 8; v++) {
+        if (dnx[v] < -1 || dnx[v] > 1 || dny[v] < -1 || dny[v] > 1) {
+            set_error("boundary table entries are -1, 0 or +1");
+            return MLAU_ERR_ARG;
+        }
+        walls |= dnx[v] != 0 || dny[v] != 0;
+    }
+    for (int v = 0; v < 8; v++) {
+        I.bcx[v] = (signed char)dnx[v];
+        I.bcy[v] = (signed char)dny[v];
+    }
+    I.walls = walls;
     return MLAU_OK;
 }
 

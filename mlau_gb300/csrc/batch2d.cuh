@@ -1,7 +1,7 @@
 // Shared definitions of the batched engine (batch2d_split.cu,
 // batch2d_plain.cu, batch1d_plain.cu, batch2d.cu).
 //
-// Many independent periodic 2D instances live in pooled per-cell arrays;
+// Many independent 2D instances live in pooled per-cell arrays;
 // instance n owns cells [base_n, base_n + nx_n*ny_n) of every pool (x fastest,
 // `off` ghost cells).  A tile table lists TW x TH cell blocks of the active
 // instances.  One persistent cooperative kernel per RK3 step runs every phase
@@ -28,6 +28,10 @@ struct BInst {
     int active, steps;
     int status, pad;  // status: 1 once a NaN or non-positive density/pressure was seen
     unsigned long long vkey;  // order-preserving key of this step's max speed
+    // 2D boundary tables (the problem's dnxs / dnys: 0 periodic, -1 Dirichlet,
+    // +1 Neumann per variable), walls: some entry is not periodic
+    int walls, pad2;
+    signed char bcx[8], bcy[8];
 };
 
 struct BTile { int inst, x0, y0, pad; };
@@ -37,6 +41,7 @@ struct BSync {
     int err, active_left;
     int ntiles, fresh;  // fresh: some 1D instance still needs its one-off dt
     BTile *tiles;
+    int walls, pad;      // some active 2D instance has non-periodic tables
 };
 
 struct BArrays {
@@ -100,6 +105,17 @@ __device__ __forceinline__ int bwrap(int i, int n, int off)
 {
     const int N = n - 2 * off;
     return (i < off) ? i + N : ((i >= n - off) ? i - N : i);
+}
+
+// Pool index of the boundary source of cell (i, j) of instance I for an
+// array with x / y table entries dnx / dny (periodic image or mirror,
+// composed over the two axes; the sign into *g), as the 2D driver's bc2d
+// (2D/SERIAL/OTvortex/boundary.c:18-74).  stx / sty: face-centred along x / y.
+__device__ __forceinline__ long long bsrc(const BInst &I, int i, int j, int stx, int sty, int dnx,
+                                          int dny, double *g)
+{
+    return I.base + (long long)I.nx * bc_src(j, I.ny, I.off, sty, dny, g) +
+           bc_src(i, I.nx, I.off, stx, dnx, g);
 }
 
 // Visit every cell of every active instance's tiles; body(I, i, j, c).

@@ -44,10 +44,19 @@ __device__ void pp_prep(const BArgs &A, int nt, const BTile *tl, int rk)
     const BArrays &a = A.a;
     for_cells(A, nt, tl, [&](const BInst &I, int i, int j, long long c) {
         const long long sy = I.nx;
-        const long long w = I.base + sy * bwrap(j, I.ny, I.off) + bwrap(i, I.nx, I.off);
+        // cell B from the face stencils at the cell's boundary source (with the
+        // tables: each component at its own source, times its sign)
+        long long wx, wy;
+        double gx = 1.0, gy = 1.0;
+        if (I.walls) {
+            wx = bsrc(I, i, j, 0, 0, I.bcx[5], I.bcy[5], &gx);
+            wy = bsrc(I, i, j, 0, 0, I.bcx[6], I.bcy[6], &gy);
+        } else {
+            wx = wy = I.base + sy * bwrap(j, I.ny, I.off) + bwrap(i, I.nx, I.off);
+        }
         const double *bx = a.s[5], *by = a.s[6];
-        const double cx = face2cen(A.odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
-        const double cy = face2cen(A.odr, by[w - sy], by[w], by[w + sy], by[w + 2 * sy]);
+        const double cx = gx * face2cen(A.odr, bx[wx - 1], bx[wx], bx[wx + 1], bx[wx + 2]);
+        const double cy = gy * face2cen(A.odr, by[wy - sy], by[wy], by[wy + sy], by[wy + 2 * sy]);
         const double ro = a.s[0][c];
         const double iro = 1.0 / ro;
         const double vx = a.s[1][c] * iro, vy = a.s[2][c] * iro, vz = a.s[3][c] * iro;
@@ -74,6 +83,14 @@ __device__ void pp_aux(const BArgs &A, int nt, const BTile *tl)
         const long long sy = I.nx;
         a.ct[c] = (i >= 1 && j >= 1) ? ct_weight(a.vx, a.vy, a.s[0], a.s[5], a.s[6], c, sy, 1, sy, 1)
                                      : 0.5;
+        if (I.walls) {  // signs of the sensors' fill (mhd_fd_ct_2d.c:262-271)
+            double g0 = 1.0, g1 = 1.0;
+            const long long w0 = bsrc(I, i, j, 0, 0, -I.bcx[1], I.bcy[1], &g0);
+            const long long w1 = bsrc(I, i, j, 0, 0, I.bcx[2], -I.bcy[2], &g1);
+            a.dv[0][c] = g0 * vmin((a.vx[w0 + 1] - a.vx[w0]), (a.vx[w0] - a.vx[w0 - 1]));
+            a.dv[1][c] = g1 * vmin((a.vy[w1 + sy] - a.vy[w1]), (a.vy[w1] - a.vy[w1 - sy]));
+            return;
+        }
         const long long w = I.base + sy * bwrap(j, I.ny, I.off) + bwrap(i, I.nx, I.off);
         a.dv[0][c] = vmin((a.vx[w + 1] - a.vx[w]), (a.vx[w] - a.vx[w - 1]));
         a.dv[1][c] = vmin((a.vy[w + sy] - a.vy[w]), (a.vy[w] - a.vy[w - sy]));
@@ -200,6 +217,11 @@ __device__ void pp_update(const BArgs &A, int nt, const BTile *tl, int rk)
             const double dd = fdiff(A.odr, ez[c - 1], ez[c], ez[c + 1], ez[c + 2]);
             out[6] = ra * a.u0[6][c] + rb * (a.s[6][c] + dtdx * dd);
         }
+        if (I.walls) {  // the boundary phases fill the ghosts
+#pragma unroll
+            for (int v = 0; v < 8; v++) a.s[v][c] = out[v];
+            return;
+        }
         const int Nx = I.nx - 2 * I.off, Ny = I.ny - 2 * I.off;
         const int is[3] = {i, i < 2 * I.off ? i + Nx : -1, i >= Nx ? i - Nx : -1};
         const int js[3] = {j, j < 2 * I.off ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -211,6 +233,46 @@ __device__ void pp_update(const BArgs &A, int nt, const BTile *tl, int rk)
 #pragma unroll
                 for (int v = 0; v < 8; v++) a.s[v][t] = out[v];
             }
+        }
+    });
+}
+
+// Instances with tables: the right boundary faces the 2D driver's CT loops
+// also update (Bx at i = nx-off, By at j = ny-off, mhd_fd_ct_2d.c:593-632),
+// where that axis mirrors the face array ...
+__device__ void pp_face(const BArgs &A, int nt, const BTile *tl, int rk)
+{
+    const BArrays &a = A.a;
+    const double rkf[3][2] = {{0.0, 1.0}, {0.5 + (3 - 2) * 0.25, 0.5 - (3 - 2) * 0.25},
+                              {1. / 3., 2. / 3.}};
+    const double ra = rkf[rk][0], rb = rkf[rk][1];
+    for_cells(A, nt, tl, [&](const BInst &I, int i, int j, long long c) {
+        if (!I.walls) return;
+        const long long sy = I.nx;
+        const double *ez = a.ez;
+        if (I.bcx[5] != 0 && i == I.nx - I.off && j >= I.off && j < I.ny - I.off) {
+            const double dd = fdiff(A.odr, ez[c - sy], ez[c], ez[c + sy], ez[c + 2 * sy]);
+            a.s[5][c] = ra * a.u0[5][c] + rb * (a.s[5][c] - (I.dt / I.dy) * dd);
+        }
+        if (I.bcy[6] != 0 && j == I.ny - I.off && i >= I.off && i < I.nx - I.off) {
+            const double dd = fdiff(A.odr, ez[c - 1], ez[c], ez[c + 1], ez[c + 2]);
+            a.s[6][c] = ra * a.u0[6][c] + rb * (a.s[6][c] + (I.dt / I.dx) * dd);
+        }
+    });
+}
+
+// ... then every ghost takes its boundary source times the signs (:636-638).
+__device__ void pp_bc(const BArgs &A, int nt, const BTile *tl)
+{
+    const BArrays &a = A.a;
+    for_cells(A, nt, tl, [&](const BInst &I, int i, int j, long long c) {
+        if (!I.walls) return;
+        if (i >= I.off && i < I.nx - I.off && j >= I.off && j < I.ny - I.off) return;
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+            double g = 1.0;
+            const long long w = bsrc(I, i, j, v == 5, v == 6, I.bcx[v], I.bcy[v], &g);
+            if (w != c) a.s[v][c] = g * a.s[v][w];
         }
     });
 }
@@ -238,6 +300,12 @@ __global__ void __launch_bounds__(256) kb_step_plain(BArgs A)
         if (grid_barrier(A.sync, A.nblocks)) return;
         pp_update(A, nt, tl, rk);
         if (grid_barrier(A.sync, A.nblocks)) return;
+        if (A.sync->walls) {
+            pp_face(A, nt, tl, rk);
+            if (grid_barrier(A.sync, A.nblocks)) return;
+            pp_bc(A, nt, tl);
+            if (grid_barrier(A.sync, A.nblocks)) return;
+        }
     }
     batch_advance(A);
 }

@@ -48,10 +48,18 @@ __device__ void ph_prep(const BArgs &A, int nt, const BTile *tl, int rk)
 {
     const BArrays &a = A.a;
     for_cells(A, nt, tl, [&](const BInst &I, int i, int j, long long c) {
-        const long long w = I.base + (long long)I.nx * bwrap(j, I.ny, I.off) + bwrap(i, I.nx, I.off);
+        long long wx, wy;
+        double gx = 1.0, gy = 1.0;
+        if (I.walls) {  // each component at its own boundary source, with its sign
+            wx = bsrc(I, i, j, 0, 0, I.bcx[5], I.bcy[5], &gx);
+            wy = bsrc(I, i, j, 0, 0, I.bcx[6], I.bcy[6], &gy);
+        } else {
+            wx = wy = I.base + (long long)I.nx * bwrap(j, I.ny, I.off) + bwrap(i, I.nx, I.off);
+        }
         const double *bx = a.s[5], *by = a.s[6];
-        const double cx = face2cen(A.odr, bx[w - 1], bx[w], bx[w + 1], bx[w + 2]);
-        const double cy = face2cen(A.odr, by[w - I.nx], by[w], by[w + I.nx], by[w + 2 * I.nx]);
+        const double cx = gx * face2cen(A.odr, bx[wx - 1], bx[wx], bx[wx + 1], bx[wx + 2]);
+        const double cy =
+            gy * face2cen(A.odr, by[wy - I.nx], by[wy], by[wy + I.nx], by[wy + 2 * I.nx]);
         const double bz = a.s[7][c];
         const double ro = a.s[0][c];
         const float2 ro2 = split2(ro);
@@ -98,6 +106,16 @@ __device__ void ph_aux(const BArgs &A, int nt, const BTile *tl)
             ctw = (va + 0.5f * eps) / (va + vb + eps);
         }
         a.ctf[c] = ctw;
+        if (I.walls) {  // signs of the sensors' fill (mhd_fd_ct_2d.c:262-271)
+            double g0 = 1.0, g1 = 1.0;
+            const long long w0 = bsrc(I, i, j, 0, 0, -I.bcx[1], I.bcy[1], &g0);
+            const long long w1 = bsrc(I, i, j, 0, 0, I.bcx[2], -I.bcy[2], &g1);
+            a.dvf[0][c] =
+                (float)g0 * fminf(pd(a.q[1][w0 + 1], a.q[1][w0]), pd(a.q[1][w0], a.q[1][w0 - 1]));
+            a.dvf[1][c] = (float)g1 *
+                          fminf(pd(a.q[2][w1 + nx], a.q[2][w1]), pd(a.q[2][w1], a.q[2][w1 - nx]));
+            return;
+        }
         const long long w = I.base + nx * bwrap(j, I.ny, I.off) + bwrap(i, I.nx, I.off);
         a.dvf[0][c] = fminf(pd(a.q[1][w + 1], a.q[1][w]), pd(a.q[1][w], a.q[1][w - 1]));
         a.dvf[1][c] = fminf(pd(a.q[2][w + nx], a.q[2][w]), pd(a.q[2][w], a.q[2][w - nx]));
@@ -302,6 +320,11 @@ __device__ void ph_update(const BArgs &A, int nt, const BTile *tl, int rk)
         const double dy_ez = d64(nx), dx_ez = d64(1);
         out[5] = ra * a.u0[5][c] + rb * (a.s[5][c] - ddy * dy_ez);
         out[6] = ra * a.u0[6][c] + rb * (a.s[6][c] + ddx * dx_ez);
+        if (I.walls) {  // the boundary phases fill the ghosts
+#pragma unroll
+            for (int v = 0; v < 8; v++) a.s[v][c] = out[v];
+            return;
+        }
         const int Nx = I.nx - 2 * I.off, Ny = I.ny - 2 * I.off;
         const int is[3] = {i, i < 2 * I.off ? i + Nx : -1, i >= Nx ? i - Nx : -1};
         const int js[3] = {j, j < 2 * I.off ? j + Ny : -1, j >= Ny ? j - Ny : -1};
@@ -313,6 +336,47 @@ __device__ void ph_update(const BArgs &A, int nt, const BTile *tl, int rk)
 #pragma unroll
                 for (int v = 0; v < 8; v++) a.s[v][t] = out[v];
             }
+        }
+    });
+}
+
+// Instances with tables: the right boundary faces the 2D driver's CT loops
+// also update (Bx at i = nx-off, By at j = ny-off, mhd_fd_ct_2d.c:593-632)
+// where that axis mirrors the face array, with the FP64 curl of ph_update ...
+__device__ void ph_face(const BArgs &A, int nt, const BTile *tl, int rk)
+{
+    const BArrays &a = A.a;
+    const double rkf[3][2] = {{0.0, 1.0}, {0.75, 0.25}, {1. / 3., 2. / 3.}};
+    const double ra = rkf[rk][0], rb = rkf[rk][1];
+    for_cells(A, nt, tl, [&](const BInst &I, int i, int j, long long c) {
+        if (!I.walls) return;
+        const float *ez = a.ezf;
+        const bool o4 = lin_odr(A.odr) > 2;
+        const double c24 = o4 ? 1.0 / 24.0 : 1.0;
+        auto d64 = [&](long long st) {
+            const double f0 = to_f64(ez[c - st]), f1 = to_f64(ez[c]), f2 = to_f64(ez[c + st]),
+                         f3 = to_f64(ez[c + 2 * st]);
+            return o4 ? 27.0 * (f2 - f1) - (f3 - f0) : f2 - f1;
+        };
+        if (I.bcx[5] != 0 && i == I.nx - I.off && j >= I.off && j < I.ny - I.off)
+            a.s[5][c] = ra * a.u0[5][c] + rb * (a.s[5][c] - I.dt / I.dy * c24 * d64(I.nx));
+        if (I.bcy[6] != 0 && j == I.ny - I.off && i >= I.off && i < I.nx - I.off)
+            a.s[6][c] = ra * a.u0[6][c] + rb * (a.s[6][c] + I.dt / I.dx * c24 * d64(1));
+    });
+}
+
+// ... then every ghost takes its boundary source times the signs (:636-638).
+__device__ void ph_bc(const BArgs &A, int nt, const BTile *tl)
+{
+    const BArrays &a = A.a;
+    for_cells(A, nt, tl, [&](const BInst &I, int i, int j, long long c) {
+        if (!I.walls) return;
+        if (i >= I.off && i < I.nx - I.off && j >= I.off && j < I.ny - I.off) return;
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+            double g = 1.0;
+            const long long w = bsrc(I, i, j, v == 5, v == 6, I.bcx[v], I.bcy[v], &g);
+            if (w != c) a.s[v][c] = g * a.s[v][w];
         }
     });
 }
@@ -341,6 +405,12 @@ __global__ void __launch_bounds__(256, 3) kb_step_split(BArgs A)
         if (grid_barrier(A.sync, A.nblocks)) return;
         ph_update(A, nt, tl, rk);
         if (grid_barrier(A.sync, A.nblocks)) return;
+        if (A.sync->walls) {
+            ph_face(A, nt, tl, rk);
+            if (grid_barrier(A.sync, A.nblocks)) return;
+            ph_bc(A, nt, tl);
+            if (grid_barrier(A.sync, A.nblocks)) return;
+        }
     }
     batch_advance(A);
 }

@@ -170,6 +170,192 @@ __global__ void k_flux1(PlainFields f, int nx, int which, double bx, double gamm
     for (int n = 0; n < 7; n++) f.F[0][n][i] = F[n];
 }
 
+// The MLAU flux (include/mhd_flux.h:26-213, point.cuh flux_mlau) of one face
+// on a lane pair: lane side 0 evaluates the left state's quantities, side 1
+// the right state's (energies, fast and "cc" speeds, the star-state
+// corrections, the boundary-normal field splits), and the pair exchanges
+// them by shuffles; the quantities that join both sides are evaluated by
+// both lanes.  Every quantity keeps flux_mlau's expression and operand
+// order, so the fluxes are its own bit for bit; a lane's chain of divisions
+// and square roots is 11 long instead of 19.
+__device__ __forceinline__ void flux_mlau_pair(const double *L, const double *R, double bnc,
+                                               double gamma, double dv0, double dv1, int side,
+                                               unsigned mask, double *f)
+{
+    const double EPS = 1e-8;
+    const double *X = side ? R : L;  // this lane's state
+    auto other = [&](double v) { return __shfl_xor_sync(mask, v, 1); };
+    auto pick = [&](double own, double oth, int want) { return side == want ? own : oth; };
+    const double rol = L[0], vnl = L[1], vtl = L[2], vul = L[3], btl = L[4], bul = L[5];
+    const double ror = R[0], vnr = R[1], vtr = R[2], vur = R[3], btr = R[4], bur = R[5];
+    const double gm1i = 1.0 / (gamma - 1.0);
+    const double bnc2 = bnc * bnc;
+    const double sgn = (bnc > 0) ? 1.0 : -1.0;
+    const double bnca = sgn * bnc;
+    // per side
+    const double roi = 1.0 / X[0];
+    const double v2 = X[1] * X[1] + X[2] * X[2] + X[3] * X[3];
+    const double pm = 0.5 * (X[4] * X[4] + X[5] * X[5]);
+    const double pt = X[6] + pm;
+    const double en = gm1i * X[6] + pm + 0.5 * X[0] * v2;
+    const double hn = (en + pt) * roi;
+    const double c2 = gamma * X[6] * roi;
+    const double ca2 = bnc2 * roi;
+    double cb2 = c2 + ca2 + 2.0 * pm * roi;
+    const double cf2 = 0.5 * (cb2 + sqrt(fabs(cb2 * cb2 - 4.0 * c2 * ca2)));
+    cb2 = v2 + ca2 + 2.0 * pm * roi;
+    const double cc2 = 0.5 * (cb2 + sqrt(fabs(cb2 * cb2 - 4.0 * v2 * ca2)));
+    const double cf2o = other(cf2), cc2o = other(cc2), pto = other(pt), hno = other(hn),
+                 roio = other(roi);
+    const double cfl2 = pick(cf2, cf2o, 0), cfr2 = pick(cf2, cf2o, 1);
+    const double ccl2 = pick(cc2, cc2o, 0), ccr2 = pick(cc2, cc2o, 1);
+    const double ptl = pick(pt, pto, 0), ptr = pick(pt, pto, 1);
+    const double hnl = pick(hn, hno, 0), hnr = pick(hn, hno, 1);
+    const double roli = pick(roi, roio, 0), rori = pick(roi, roio, 1);
+    // joint
+    const double cmax = sqrt(vmax(cfl2, cfr2));
+    const double cfn = cmax;
+    const double cfni = 1.0 / cfn;
+    const double sl = vmin(0.0, vmin(vnl, vnr) - cmax);
+    const double sr = vmax(0.0, vmax(vnl, vnr) + cmax);
+    const double mal = vnl * cfni, mar = vnr * cfni;
+    const double snl = (mal > 0) ? 1.0 : -1.0;
+    const double snr = (mar > 0) ? 1.0 : -1.0;
+    double theta = vmin(1.0, (cfn - vmin(dv0, 0.0)) / (cfn - vmin(dv1, 0.0)));
+    theta *= theta;
+    theta *= theta;
+    const double alpha = 0.1875, beta = 0.125;
+    const double malp1 = mal + 1.0, marm1 = mar - 1.0;
+    const double mal2m1 = mal * mal - 1.0, mar2m1 = mar * mar - 1.0;
+    double bfl, ffl, bfr, ffr;
+    if (snl * mal > 1.0) {
+        bfl = 0.5 * (1.0 + snl);
+        ffl = bfl * mal;
+    } else {
+        bfl = +0.25 * malp1 * malp1 * (2.0 - mal) + alpha * mal * mal2m1 * mal2m1;
+        ffl = +0.25 * malp1 * malp1 + beta * mal2m1 * mal2m1;
+    }
+    if (snr * mar > 1.0) {
+        bfr = 0.5 * (1.0 - snr);
+        ffr = bfr * mar;
+    } else {
+        bfr = +0.25 * marm1 * marm1 * (2.0 + mar) - alpha * mar * mar2m1 * mar2m1;
+        ffr = -0.25 * marm1 * marm1 - beta * mar2m1 * mar2m1;
+    }
+    const double mnc = ffl + ffr;
+    double mflux = mnc * cfn;
+    const double dpt = ptr - ptl;
+    const double dvn = vnr - vnl;
+    mflux -= vmax(1.0 - fabs(mnc), 0.0) * theta * cfni * dpt / (rol + ror);
+    const double dir = (mflux > 0) ? 1.0 : -1.0;
+    const double dirl = 0.5 * (1.0 + dir);
+    const double dirr = 1.0 - dirl;
+    mflux *= (dirl * rol + dirr * ror);
+    const double mfl = mflux * dirl;
+    const double mfr = mflux - mfl;
+    double ptot = bfl * ptl + bfr * ptr;
+    const double cfmod = sqrt(vmax(ccl2, ccr2));
+    ptot -= 0.25 * bfl * bfr * (rol + ror) * cfmod * dvn;
+    ptot -= 0.5 * (1.0 - cfmod * cfni) * (bfl + bfr - 1.0) * (ptl + ptr);
+    const double slvl = sl - vnl, srvr = sr - vnr;
+    const double snc = dirl * sl + dirr * sr;
+    const double vndnm = mflux + dirl * rol * slvl + dirr * ror * srvr;
+    const double vnc = ((fabs(vndnm) > EPS) && (snc != 0)) ? (mflux * snc / vndnm)
+                                                          : (dirl * vnl + dirr * vnr);
+    const double slvc = sl - vnc, srvc = sr - vnc;
+    // per side: star-state corrections
+    const double svX = side ? srvr : slvl, svc = side ? srvc : slvc;
+    const double svci = 1.0 / svc;
+    const double rhd = X[0] * svX * svc - bnc2;
+    double dvt = 0.0, dvu = 0.0, dbt = 0.0, dbu = 0.0;
+    if (fabs(rhd) > EPS) {
+        const double g = (vnc - X[1]) / rhd;
+        dvt = -bnc * X[4] * g;
+        dvu = -bnc * X[5] * g;
+        dbt = bnc2 * X[4] * g * svci;
+        dbu = bnc2 * X[5] * g * svci;
+    }
+    const double cmp = svX * svci;
+    const double ro2 = X[0] * cmp;
+    const double sro = sqrt(ro2);
+    const double vt2 = dvt + X[2], vu2 = dvu + X[3];
+    const double bt2 = dbt + X[4] * cmp, bu2 = dbu + X[5] * cmp;
+    const double o_svci = other(svci), o_sro = other(sro), o_vt2 = other(vt2),
+                 o_vu2 = other(vu2), o_bt2 = other(bt2), o_bu2 = other(bu2), o_dvt = other(dvt),
+                 o_dvu = other(dvu), o_dbt = other(dbt), o_dbu = other(dbu);
+    const double slvci = pick(svci, o_svci, 0), srvci = pick(svci, o_svci, 1);
+    const double srol = pick(sro, o_sro, 0), sror = pick(sro, o_sro, 1);
+    const double vt2l = pick(vt2, o_vt2, 0), vt2r = pick(vt2, o_vt2, 1);
+    const double vu2l = pick(vu2, o_vu2, 0), vu2r = pick(vu2, o_vu2, 1);
+    const double bt2l = pick(bt2, o_bt2, 0), bt2r = pick(bt2, o_bt2, 1);
+    const double bu2l = pick(bu2, o_bu2, 0), bu2r = pick(bu2, o_bu2, 1);
+    const double dvtl = pick(dvt, o_dvt, 0), dvtr = pick(dvt, o_dvt, 1);
+    const double dvul = pick(dvu, o_dvu, 0), dvur = pick(dvu, o_dvu, 1);
+    const double dbtl = pick(dbt, o_dbt, 0), dbtr = pick(dbt, o_dbt, 1);
+    const double dbul = pick(dbu, o_dbu, 0), dbur = pick(dbu, o_dbu, 1);
+    // joint
+    const double sroi = 1.0 / (srol + sror);
+    const double srollri = srol * sroi, srorlri = sror * sroi;
+    const double bnflb = sgn * vmin(vmax(0.0, srollri * (bnca + sror * vnc)), bnca);
+    const double bnfrb = sgn * vmin(vmax(0.0, srorlri * (bnca - srol * vnc)), bnca);
+    // the two velocity-side splits, one per lane
+    const double bnfv = side ? sgn * vmin(vmax(0.0, srollri * (bnca - mflux / srol)), bnca)
+                             : sgn * vmin(vmax(0.0, srorlri * (bnca + mflux / sror)), bnca);
+    const double o_bnfv = other(bnfv);
+    const double bnflv = pick(bnfv, o_bnfv, 0), bnfrv = pick(bnfv, o_bnfv, 1);
+    const double bnsrv = vmax(bnca - dir * vnc * (dirl * srol + dirr * sror), 0.0);
+    const double ccb = sroi * bnsrv;
+    const double ccv = srol * sror * ccb;
+    double bnvt = bnflb * vt2l + bnfrb * vt2r + ccb * (bt2r - bt2l);
+    double bnvu = bnflb * vu2l + bnfrb * vu2r + ccb * (bu2r - bu2l);
+    double bnbt = bnflv * bt2l + bnfrv * bt2r + ccv * (vt2r - vt2l);
+    double bnbu = bnflv * bu2l + bnfrv * bu2r + ccv * (vu2r - vu2l);
+    bnvt -= vnc * (dirl * dbtl + dirr * dbtr);
+    bnvu -= vnc * (dirl * dbul + dirr * dbur);
+    bnbt -= mflux * (dirl * dvtl + dirr * dvtr);
+    bnbu -= mflux * (dirl * dvul + dirr * dvur);
+    f[0] = mflux;
+    f[1] = mfl * vnl + mfr * vnr + ptot - 0.5 * bnc2;
+    f[2] = mfl * vtl + mfr * vtr - bnbt;
+    f[3] = mfl * vul + mfr * vur - bnbu;
+    f[4] = mfl * btl * roli + mfr * btr * rori - bnvt;
+    f[5] = mfl * bul * roli + mfr * bur * rori - bnvu;
+    const double vb1 = dirl * (vtl * btl + vul * bul) + dirr * (vtr * btr + vur * bur);
+    const double vb2 = dirl * (vt2l * bt2l + vu2l * bu2l) + dirr * (vt2r * bt2r + vu2r * bu2r);
+    double rv2b2 = (mflux * vnc - bnc2);
+    rv2b2 *= rv2b2;
+    double vb3 = 0.0;
+    if (rv2b2 > EPS * EPS) {
+        vb3 = (+(f[2] * vnc + f[4] * bnc) * (f[2] * bnc + f[4] * mflux)
+               + (f[3] * vnc + f[5] * bnc) * (f[3] * bnc + f[5] * mflux)) / rv2b2;
+    }
+    const double bnvb = sgn * (bnca * (snc * vb2 - vnc * vb1) * (dirl * slvci + dirr * srvci)
+                               + bnsrv * (vb3 - vb2));
+    f[6] = mfl * hnl + mfr * hnr - bnvb;
+}
+
+// MLAU faces on lane pairs (flux_mlau_pair); the other solvers keep one
+// face per thread (k_flux1).
+__global__ void k_flux1_mlau(PlainFields f, int nx, double bx, double gamma)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int side = t & 1, i = 3 + t / 2;
+    const bool live = i < nx - 2;
+    const int ic = live ? i : nx - 3;  // both lanes of a pair take part in the shuffles
+    const unsigned mask = blockDim.x >= 32 ? 0xffffffffu : (1u << blockDim.x) - 1u;
+    double L[7], R[7], F[7];
+#pragma unroll
+    for (int n = 0; n < 7; n++) {
+        L[n] = f.ul[n][ic];
+        R[n] = f.ur[n][ic];
+    }
+    flux_mlau_pair(L, R, bx, gamma, (f.vx[ic] - f.vx[ic - 1]), 0.0, side, mask, F);
+    if (!live) return;
+#pragma unroll
+    for (int n = 0; n < 7; n++)
+        if ((n < 4) == (side == 0)) f.F[0][n][i] = F[n];
+}
+
 // openbc1d_mhd (1D/SERIAL/shock/openbc1d_mhd.c:21-175).  The two sides read
 // and write disjoint cells (interior width >= ghost depth), so each runs in
 // its own block of 8 lanes: block 0 the left side, block 1 the right.  Lane r
@@ -315,7 +501,11 @@ int plain1d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_FLUX);
-            k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, s->flux, s->bx1d, s->gamma);
+            if (s->flux == FLUX_MLAU)
+                k_flux1_mlau<<<blocks_for((long long)(nx - 5) * 2, T), T, 0, st>>>(f, nx, s->bx1d,
+                                                                                s->gamma);
+            else
+                k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, s->flux, s->bx1d, s->gamma);
         }
         if (s->bc1d == MLAU_BC1D_OPEN && rk == 0) {
             TimedLaunch tl(&s->timer, KK_AUX);
@@ -349,7 +539,10 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
         k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma, rk == 0);
         k_rec1<<<blocks_for((long long)(nx - 4) * RLANES, T), T, 0, st>>>(f, nx, odr, EIG_FULL,
                                                                         bx, gamma);
-        k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
+        if (flux == FLUX_MLAU)
+            k_flux1_mlau<<<blocks_for((long long)(nx - 5) * 2, T), T, 0, st>>>(f, nx, bx, gamma);
+        else
+            k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
         if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<2, 8, 0, st>>>(f, nx, off, bx, dtdx, gamma);
         k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(f, nx, off, odr, ra, rb, dtdx,
                                                             bc == MLAU_BC1D_PERIODIC);

@@ -344,3 +344,99 @@ def test_split_runs_a_marginal_request_to_its_end_like_fp64():
             assert not b.failed(s), prec
             assert t == pytest.approx(m["t_end"], rel=1e-12)
     assert abs(steps[M.FP32_SPLIT] - steps[M.FP64]) <= 2
+
+
+# --- boundary tables in the batched engines -----------------------------------
+KHI = ((0,) * 8, (1, 1, -1, 1, 1, 1, -1, 1))  # 2D/MPI/KHI/global.hpp:21-22
+XWALLS = ((1, -1, 1, 1, 1, -1, 1, 1), (0,) * 8)
+BOTH = ((1, -1, 1, 1, 1, -1, 1, 1), (1, 1, -1, 1, 1, 1, -1, 1))
+PERIODIC = ((0,) * 8, (0,) * 8)
+WALL_CASES = [((24, 18), KHI, "lhlld"), ((32, 24), XWALLS, "mlau"), ((20, 28), BOTH, "hlld"),
+              ((28, 20), PERIODIC, "mlau"), ((26, 22), KHI, "mlau")]
+
+
+def wall_cases(port, seed=41):
+    out = []
+    for k, (shape, tables, flux) in enumerate(WALL_CASES):
+        st, m = ics.turbulence_2d(n=shape[0], ny=shape[1], seed=seed + k, vrms=0.4)
+        port.setbc2d(st, *tables)
+        out.append(dict(st=st, m=m, tables=tables, flux=flux))
+    return out
+
+
+def test_fp64_engine_with_tables_equals_single_instance(port):
+    """FP64 engine, instances with different tables (KHI's reflecting y walls,
+    x walls, both, periodic) in one batch: each advances bit for bit like the
+    single-instance 2D step with the same tables, CFL dt every step."""
+    cases = wall_cases(port)
+    refs = []
+    for c in cases:
+        m = c["m"]
+        with M.Sim(2, c["st"]["ro"].shape, dx=m["dx"], dy=m["dy"], gamma=m["gamma"], odr=4,
+                   flux=c["flux"]) as s:
+            s.set_bc2d(*c["tables"])
+            s.upload(c["st"])
+            for _ in range(5):
+                dt, _ = s.cfl(0.4, min(m["dx"], m["dy"]), 0.0, 0.0)
+                s.step(dt, 1)
+            refs.append(s.download())
+    cells = sum(c["st"]["ro"].size for c in cases)
+    with M.Batch.open(cells, 8, precision=M.FP64) as b:
+        slots = []
+        for c in cases:
+            k = b.add(c["st"], c["m"]["dx"], c["m"]["dy"], c["m"]["gamma"], c["flux"], 0.4, 10.0)
+            b.set_bc(k, *c["tables"])
+            slots.append(k)
+        b.run(5, steps_per_graph=2)
+        for k, sl in enumerate(slots):
+            got = b.download(sl)
+            for v in got:
+                assert np.array_equal(got[v], refs[k][v]), (k, v)
+
+
+def div_b_2d_change(st, base, m, margin):
+    """max |div B - div B(base)| * dx / max |B| over the cells `margin` (y, x)
+    cells away from each end (4th-order differences)."""
+    def d(f, ax, h):
+        f2 = np.roll(f, -1, axis=ax)
+        return (27.0 * (f2 - f) - (np.roll(f, -2, axis=ax) - np.roll(f, 1, axis=ax))) / 24.0 / h
+    def div(s):
+        return d(s["bx"], 1, m["dx"]) + d(s["by"], 0, m["dy"])
+    sl = tuple(slice(a, -a) for a in margin)
+    bmax = max(np.abs(st[k][INT2]).max() for k in ("bx", "by"))
+    return float(np.abs((div(st) - div(base))[sl]).max() * min(m["dx"], m["dy"]) / bmax)
+
+
+def test_split_engine_with_tables_vs_fp64(port):
+    """FP32-split engine with the same mix of tables against the FP64 engine:
+    relative L1 over every cell (ghosts included) <= 1e-6 for density and
+    energy and <= 1e-5 for face B; div B (from the first step on) at
+    round-off two or more cells away from a mirror wall, and within 1e-9 next
+    to one (the ghost faces are mirror copies and the FP32 EMFs there are
+    mirror-symmetric only to FP32 rounding)."""
+    cases = wall_cases(port, seed=53)
+    cells = sum(c["st"]["ro"].size for c in cases)
+    out = {}
+    for prec in (M.FP64, M.FP32_SPLIT):
+        with M.Batch.open(cells, 8, precision=prec) as b:
+            slots = []
+            for c in cases:
+                k = b.add(c["st"], c["m"]["dx"], c["m"]["dy"], c["m"]["gamma"], c["flux"], 0.4,
+                          10.0)
+                b.set_bc(k, *c["tables"])
+                b.set_fixed_dt(k, 0.3 * c["m"]["dx"] / c["m"]["vfast"])
+                slots.append(k)
+            b.run(1)
+            first = [b.download(k) for k in slots]
+            b.run(19)
+            out[prec] = (first, [b.download(k) for k in slots])
+    for k, c in enumerate(cases):
+        ref, got, f1 = out[M.FP64][1][k], out[M.FP32_SPLIT][1][k], out[M.FP32_SPLIT][0][k]
+        for v, tol in (("ro", 1e-6), ("en", 1e-6), ("bx", 1e-5), ("by", 1e-5)):
+            assert np.isfinite(got[v]).all(), (k, v)
+            err = np.abs(got[v] - ref[v]).sum() / np.abs(ref[v]).sum()
+            assert err <= tol, (k, v, err)
+        walls = [any(t) for t in c["tables"]]  # x, y
+        margin = tuple(6 if w else 4 for w in walls[::-1])
+        assert div_b_2d_change(got, f1, c["m"], margin) <= 1e-12, k
+        assert div_b_2d_change(got, f1, c["m"], (4, 4)) <= 1e-9, k
