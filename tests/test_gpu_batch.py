@@ -355,10 +355,13 @@ WALL_CASES = [((24, 18), KHI, "lhlld"), ((32, 24), XWALLS, "mlau"), ((20, 28), B
               ((28, 20), PERIODIC, "mlau"), ((26, 22), KHI, "mlau")]
 
 
-def wall_cases(port, seed=41):
+def wall_cases(port, seed=72):
+    """States whose pressure stays positive over the tests' 20 steps with
+    these tables (checked with the oracle; the engine retires an instance
+    whose pressure goes non-positive, the single-instance step does not)."""
     out = []
     for k, (shape, tables, flux) in enumerate(WALL_CASES):
-        st, m = ics.turbulence_2d(n=shape[0], ny=shape[1], seed=seed + k, vrms=0.4)
+        st, m = ics.turbulence_2d(n=shape[0], ny=shape[1], seed=seed + k, vrms=0.25)
         port.setbc2d(st, *tables)
         out.append(dict(st=st, m=m, tables=tables, flux=flux))
     return out
@@ -414,7 +417,7 @@ def test_split_engine_with_tables_vs_fp64(port):
     round-off two or more cells away from a mirror wall, and within 1e-9 next
     to one (the ghost faces are mirror copies and the FP32 EMFs there are
     mirror-symmetric only to FP32 rounding)."""
-    cases = wall_cases(port, seed=53)
+    cases = wall_cases(port)
     cells = sum(c["st"]["ro"].size for c in cases)
     out = {}
     for prec in (M.FP64, M.FP32_SPLIT):
