@@ -355,7 +355,7 @@ WALL_CASES = [((24, 18), KHI, "lhlld"), ((32, 24), XWALLS, "mlau"), ((20, 28), B
               ((28, 20), PERIODIC, "mlau"), ((26, 22), KHI, "mlau")]
 
 
-def wall_cases(port, seed=72):
+def wall_cases(port, seed=76):
     """States whose pressure stays positive over the tests' 20 steps with
     these tables (checked with the oracle; the engine retires an instance
     whose pressure goes non-positive, the single-instance step does not)."""
