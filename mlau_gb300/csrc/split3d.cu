@@ -52,8 +52,11 @@
 #include "split_conv.cuh"
 #include "ff.cuh"
 #include "point_x2.cuh"
+#include "slab_plan.h"
 
 #include <algorithm>
+#include <memory>
+#include <vector>
 
 namespace mlau {
 
@@ -92,9 +95,13 @@ struct SplitFields {
     int spec = 0;           // sweep instance: 0 run-time scheme, 1 WCNS4 + MLAU, 2 WCNS4 + LHLLD
     int f64 = 0;            // state arithmetic in FP64 (MLAU_FP32_SPLIT_F64), else float-float
     int *d_err = nullptr;   // set when a bounded wait gave up
-    // host-array steps (split3d_step_host): copy stream and slab events
-    cudaStream_t cs = nullptr;
-    cudaEvent_t ev_in[8] = {}, ev_out[8] = {};
+    // host-array steps (split3d_step_host): upload / download streams, the
+    // plane schedule and its copy events
+    cudaStream_t cs = nullptr, cd = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    std::unique_ptr<SlabPlan> plan;
+    int plan_nrk = 0;
+    std::vector<cudaEvent_t> ev_up, ev_dn;
 };
 
 namespace {
@@ -114,10 +121,9 @@ struct Dims {
     }
 };
 
-// Cell of this thread for the whole-grid kernels: one thread per cell of an
-// x-y plane (flattened, so no block runs mostly past the row end), one grid
-// row of blocks per z-plane.
-// row of blocks per z-plane, from plane k0.
+// Cell of this thread for the plane kernels: one thread per cell of an x-y
+// plane (flattened, so no block runs mostly past the row end), one grid row
+// of blocks per z-plane, from plane k0.
 __device__ __forceinline__ bool plane_cell(const Dims &d, int &i, int &j, int &k, int k0 = 0)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -278,10 +284,10 @@ __device__ __forceinline__ float ct_w(const float2 *va, const float2 *vb, const 
 // as the reference fills them (mhd_fd_ct_3d.c:367-376: dvx takes -dnxs[1]
 // along x, dvy -dnys[2] along y, dvz -dnzs[3] along z).
 template <bool WALLS>
-__global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d, Bc3 bc)
+__global__ void __launch_bounds__(256) ks_aux(SplitPtrs g, Dims d, Bc3 bc, int k0)
 {
     int i, j, k;
-    if (!plane_cell(d, i, j, k)) return;
+    if (!plane_cell(d, i, j, k, k0)) return;
     const long long sy = d.px, sz = d.px * d.ny;
     const long long s = d.ap(i, j, k);
     const float2 *ro = g.q[0], *vx = g.q[1], *vy = g.q[2], *vz = g.q[3];
@@ -347,7 +353,9 @@ struct TileAt {
 };
 
 // Tile t of a sweep: n0 tiles along the first tile axis, n1 along the second.
-template <int D> __device__ __forceinline__ TileAt tile_at(int t, int n0, int n1)
+// A launch over part of the grid starts its z-planes (D = 0, 1) or its tile
+// rows along z (D = 2) at base.
+template <int D> __device__ __forceinline__ TileAt tile_at(int t, int n0, int n1, int base)
 {
     constexpr int T = SG<D>::T;
     const int t0 = t % n0, r = t / n0, t1 = r % n1, t2 = r / n1;
@@ -356,18 +364,18 @@ template <int D> __device__ __forceinline__ TileAt tile_at(int t, int n0, int n1
         const int x0 = 2 + (T - 1) * t0;
         a.x = (x0 - 2) & ~3;
         a.y = SG<0>::TB * t1;
-        a.z = t2;
-        a.i0 = x0; a.j0 = a.y; a.k0 = t2;
+        a.z = base + t2;
+        a.i0 = x0; a.j0 = a.y; a.k0 = a.z;
         a.off = x0 - a.x;
     } else if (D == 1) {
         const int y0 = 2 + (T - 1) * t1;
         a.x = SG<1>::TA * t0;
         a.y = y0 - 2;
-        a.z = t2;
-        a.i0 = a.x; a.j0 = y0; a.k0 = t2;
+        a.z = base + t2;
+        a.i0 = a.x; a.j0 = y0; a.k0 = a.z;
         a.off = 0;
     } else {
-        const int z0 = 2 + (T - 1) * t1;
+        const int z0 = 2 + (T - 1) * (base + t1);
         a.x = SG<2>::TA * t0;
         a.y = t2;
         a.z = z0 - 2;
@@ -541,7 +549,7 @@ __device__ __forceinline__ void rec_cell_wcns4(const float2 *Q, const float *Fs,
 template <int D, int ODR = 0, int WHICH = -1>
 __global__ void __launch_bounds__(SG<D>::TA *SG<D>::TB, ODR ? 5 : 1)
 ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, int which_rt,
-         float gamma, int n0, int n1, int ntiles, int *err)
+         float gamma, int n0, int n1, int ntiles, int base, int *err)
 {
     const int odr = ODR ? ODR : odr_rt;
     const int which = WHICH >= 0 ? WHICH : which_rt;
@@ -566,7 +574,7 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
     }
     __syncthreads();
     if (tid == 0 && (int)blockIdx.x < ntiles)
-        issue_tile<D>(M, stages, tile_at<D>(blockIdx.x, n0, n1), &bar[0]);
+        issue_tile<D>(M, stages, tile_at<D>(blockIdx.x, n0, n1, base), &bar[0]);
 
     int it = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
@@ -576,7 +584,7 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
             // the other buffer was released by the barrier that ended the
             // previous iteration
             fence_async_shared();
-            issue_tile<D>(M, stages + (b ^ 1) * STAGE, tile_at<D>(tn, n0, n1), &bar[b ^ 1]);
+            issue_tile<D>(M, stages + (b ^ 1) * STAGE, tile_at<D>(tn, n0, n1, base), &bar[b ^ 1]);
         }
         const bool ok = mbar_wait(&bar[b], (it >> 1) & 1);
         if (__syncthreads_or(!ok)) {
@@ -588,7 +596,7 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
         }
         const float2 *Q = (const float2 *)(stages + b * STAGE);
         const float *Fs = (const float *)(stages + b * STAGE + NQ * NB * sizeof(float2));
-        const TileAt a = tile_at<D>(t, n0, n1);
+        const TileAt a = tile_at<D>(t, n0, n1, base);
         const int i = a.i0 + ta, j = a.j0 + ((D == 2) ? 0 : tb), k = a.k0 + ((D == 2) ? tb : 0);
         const int ac = (D == 0) ? i : (D == 1 ? j : k);  // sweep coordinate
         const bool in_box = i < d.nx && j < d.ny && k < d.nz;
@@ -657,10 +665,10 @@ __device__ __forceinline__ float emf_part32(const float *fu, const float *fc, fl
     return h * ((ul0 + ur0) + w * (ul1 + ur1));
 }
 
-__global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr)
+__global__ void __launch_bounds__(256) ks_emf(SplitPtrs g, Dims d, int odr, int k0)
 {
     int i, j, k;
-    if (!plane_cell(d, i, j, k)) return;
+    if (!plane_cell(d, i, j, k, k0)) return;
     const long long sy = d.px, sz = d.px * d.ny;
     const long long c = d.ap(i, j, k);
     const bool xi = (i >= 3 && i < d.nx - 2), yj = (j >= 3 && j < d.ny - 2),
@@ -936,23 +944,35 @@ template <int D> int setup_sweep(Sim *s, SplitFields &sf)
     return MLAU_OK;
 }
 
+// Sweep D over the whole grid (count < 0), or over z-planes [base, base +
+// count) (D = 0, 1) / tile rows along z [base, base + count) (D = 2).
 template <int D>
-void launch_sweep(Sim *s, SplitFields &sf, const Dims &d, float gam)
+void launch_sweep(Sim *s, SplitFields &sf, const Dims &d, float gam, int base = 0,
+                  int count = -1)
 {
     const dim3 b(SG<D>::TA, SG<D>::TB);
     const size_t dyn = sweep_dyn_smem<D>();
+    const int n0 = sf.ntile[D][0];
+    int n1 = sf.ntile[D][1], ntiles = sf.ntiles[D];
+    if (count >= 0) {
+        if (D == 2) {
+            n1 = count;
+            ntiles = n0 * count * d.ny;
+        } else {
+            ntiles = n0 * n1 * count;
+        }
+    }
+    if (ntiles <= 0) return;
+    const int nb = std::min(ntiles, sf.nblocks[D]);
     if (sf.spec == 1)
-        ks_sweep<D, 4, FLUX_MLAU><<<sf.nblocks[D], b, dyn, s->stream>>>(
-            sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1],
-            sf.ntiles[D], sf.d_err);
+        ks_sweep<D, 4, FLUX_MLAU><<<nb, b, dyn, s->stream>>>(
+            sf.maps[D], sf.p, d, s->odr, s->flux, gam, n0, n1, ntiles, base, sf.d_err);
     else if (sf.spec == 2)
-        ks_sweep<D, 4, FLUX_LHLLD><<<sf.nblocks[D], b, dyn, s->stream>>>(
-            sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1],
-            sf.ntiles[D], sf.d_err);
+        ks_sweep<D, 4, FLUX_LHLLD><<<nb, b, dyn, s->stream>>>(
+            sf.maps[D], sf.p, d, s->odr, s->flux, gam, n0, n1, ntiles, base, sf.d_err);
     else
-        ks_sweep<D><<<sf.nblocks[D], b, dyn, s->stream>>>(
-            sf.maps[D], sf.p, d, s->odr, s->flux, gam, sf.ntile[D][0], sf.ntile[D][1],
-            sf.ntiles[D], sf.d_err);
+        ks_sweep<D><<<nb, b, dyn, s->stream>>>(sf.maps[D], sf.p, d, s->odr, s->flux, gam, n0,
+                                               n1, ntiles, base, sf.d_err);
 }
 
 }  // namespace
@@ -1034,11 +1054,12 @@ void split3d_free(Sim *s)
     SplitFields *sf = s->sp;
     if (sf && sf->cs) {
         cudaStreamSynchronize(sf->cs);
-        for (int c = 0; c < 8; c++) {
-            cudaEventDestroy(sf->ev_in[c]);
-            cudaEventDestroy(sf->ev_out[c]);
-        }
+        cudaStreamSynchronize(sf->cd);
+        for (cudaEvent_t e : sf->ev_up) cudaEventDestroy(e);
+        for (cudaEvent_t e : sf->ev_dn) cudaEventDestroy(e);
+        cudaEventDestroy(sf->ev_start);
         cudaStreamDestroy(sf->cs);
+        cudaStreamDestroy(sf->cd);
     }
     delete sf;
     s->sp = nullptr;
@@ -1081,10 +1102,11 @@ struct StepCtx {
                                                    host_ff(s->gamma - 1), s->gamma - 1,
                                                    (float)s->gamma, rk == 0, k0);
     }
-    void aux() const
+    // CT weights and shock sensors of planes [k0, k0 + nk)
+    void aux(int k0, int nk) const
     {
         auto kern = s->walls3d ? ks_aux<true> : ks_aux<false>;
-        kern<<<cg, cb, 0, s->stream>>>(s->sp->p, d, s->bc3);
+        kern<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->sp->p, d, s->bc3, k0);
     }
     void sweeps() const
     {
@@ -1093,7 +1115,18 @@ struct StepCtx {
         launch_sweep<1>(s, *s->sp, d, gam);
         launch_sweep<2>(s, *s->sp, d, gam);
     }
-    void emf() const { ks_emf<<<cg, cb, 0, s->stream>>>(s->sp->p, d, s->odr); }
+    // sweep D over planes (D = 0, 1) or tile rows along z (D = 2) [a, b)
+    void sweep(int D, int a, int b) const
+    {
+        const float gam = (float)s->gamma;
+        if (D == 0) launch_sweep<0>(s, *s->sp, d, gam, a, b - a);
+        else if (D == 1) launch_sweep<1>(s, *s->sp, d, gam, a, b - a);
+        else launch_sweep<2>(s, *s->sp, d, gam, a, b - a);
+    }
+    void emf(int k0, int nk) const
+    {
+        ks_emf<<<dim3(cg.x, nk), cb, 0, s->stream>>>(s->sp->p, d, s->odr, k0);
+    }
     // RK combine + CT curl of the interior planes [k0, k0 + nk)
     void update(int rk, double dt, int k0, int nk) const
     {
@@ -1132,7 +1165,7 @@ int split3d_step(Sim *s, double dt)
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_PREP);
             x.prim(rk, 0, G.nz);
-            x.aux();
+            x.aux(0, G.nz);
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_SWEEP);
@@ -1140,7 +1173,7 @@ int split3d_step(Sim *s, double dt)
         }
         {
             TimedLaunch tl(&s->timer, KK_EMF);
-            x.emf();
+            x.emf(0, G.nz);
         }
         {
             TimedLaunch tl(&s->timer, KK_SPLIT_UPDATE);
@@ -1151,81 +1184,90 @@ int split3d_step(Sim *s, double dt)
     return MLAU_OK;
 }
 
-// One step of a state held in host arrays h[0..7] (the C-ABI drivers), in
-// place: the same kernels and arithmetic as upload + split3d_step + download,
-// with the host link's copies overlapped where the data allow.  The upload
-// goes in z-slabs on a copy stream, and the first stage's primitive recovery
-// of each slab starts once the slab above it is in (it reads face B up to two
-// planes up; the slabs holding ghost planes read their periodic sources at
-// the far end and wait for the whole state).  The last stage's update runs
-// slab by slab, and each slab's interior planes go back to the host while the
-// next slab updates; the ghost planes, which receive the periodic images
-// written by the update of the far end, go last.
+// One step of a periodic state held in host arrays h[0..7] (the C-ABI
+// drivers), in place: the same kernels and arithmetic as upload +
+// split3d_step + download, run over z-plane ranges in the order of a
+// SlabPlan (slab_plan.h), so that the upload overlaps the first RK stage and
+// the download the last.  Uploads go in chunks of planes on one copy stream,
+// each recorded by an event the compute stream waits on before the first
+// kernel that reads those planes; downloads go on a second copy stream, each
+// run of planes as soon as the update that writes it has been launched.
 int split3d_step_host(Sim *s, double dt, double *const *h)
 {
     const Geometry &G = s->g;
     SplitFields &sf = *s->sp;
+    const int nz = G.nz, oz = G.oz, Nz = nz - 2 * oz;
     if (!sf.cs) {
         MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cs, cudaStreamNonBlocking));
-        for (int c = 0; c < 8; c++) {
-            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_in[c], cudaEventDisableTiming));
-            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_out[c], cudaEventDisableTiming));
+        MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cd, cudaStreamNonBlocking));
+        MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_start, cudaEventDisableTiming));
+    }
+    if (!sf.plan || sf.plan_nrk != s->nrk) {
+        // the first and last stages are asked for in slabs of >= 16 interior
+        // planes (at most 8); uploads of half a slab
+        const int nslab = std::max(1, std::min(8, Nz / 16));
+        const int chunk = std::max(4, (nz + 2 * nslab - 1) / (2 * nslab));
+        sf.plan.reset(new SlabPlan(SlabGeom{nz, oz, SG<2>::T}, s->nrk, nslab, chunk));
+        sf.plan_nrk = s->nrk;
+        int ndn = 0;
+        for (const SlabOp &o : sf.plan->ops) ndn += o.kind == SP_DOWNLOAD;
+        for (size_t e = sf.ev_up.size(); e < (size_t)sf.plan->uploads(); e++) {
+            sf.ev_up.push_back(nullptr);
+            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_up.back(), cudaEventDisableTiming));
+        }
+        for (size_t e = sf.ev_dn.size(); e < (size_t)ndn; e++) {
+            sf.ev_dn.push_back(nullptr);
+            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_dn.back(), cudaEventDisableTiming));
         }
     }
-    const int nz = G.nz, oz = G.oz, Nz = nz - 2 * oz;
     const long long plane = (long long)G.nx * G.ny;
-    const int ns = std::max(1, std::min(8, Nz / 8));  // slabs of >= 8 interior planes
-    int b[9];  // slab c: planes [b[c], b[c + 1]); ghost planes with the end slabs
-    b[0] = 0;
-    for (int c = 1; c < ns; c++) b[c] = oz + (int)((long long)Nz * c / ns);
-    b[ns] = nz;
-    auto copy = [&](int k0, int k1, bool in) -> int {
+    auto copy = [&](cudaStream_t st, int k0, int k1, bool in) -> int {
         for (int v = 0; v < 8; v++) {
             double *dv = s->f.s[v] + k0 * plane, *hv = h[v] + k0 * plane;
             const size_t bytes = sizeof(double) * (size_t)(k1 - k0) * plane;
-            MLAU_CUDA(in ? cudaMemcpyAsync(dv, hv, bytes, cudaMemcpyHostToDevice, sf.cs)
-                         : cudaMemcpyAsync(hv, dv, bytes, cudaMemcpyDeviceToHost, sf.cs));
+            MLAU_CUDA(in ? cudaMemcpyAsync(dv, hv, bytes, cudaMemcpyHostToDevice, st)
+                         : cudaMemcpyAsync(hv, dv, bytes, cudaMemcpyDeviceToHost, st));
         }
         return MLAU_OK;
     };
     // the previous use of the state on the compute stream ends before the upload
-    MLAU_CUDA(cudaEventRecord(sf.ev_out[0], s->stream));
-    MLAU_CUDA(cudaStreamWaitEvent(sf.cs, sf.ev_out[0], 0));
-    for (int c = 0; c < ns; c++) {
-        if (int rc = copy(b[c], b[c + 1], true)) return rc;
-        MLAU_CUDA(cudaEventRecord(sf.ev_in[c], sf.cs));
-    }
+    MLAU_CUDA(cudaEventRecord(sf.ev_start, s->stream));
+    MLAU_CUDA(cudaStreamWaitEvent(sf.cs, sf.ev_start, 0));
     const StepCtx x(s);
-    for (int rk = 0; rk < s->nrk; rk++) {
-        if (rk == 0) {
-            for (int c = 1; c + 1 < ns; c++) {
-                MLAU_CUDA(cudaStreamWaitEvent(s->stream, sf.ev_in[c + 1], 0));
-                x.prim(0, b[c], b[c + 1] - b[c]);
-            }
-            MLAU_CUDA(cudaStreamWaitEvent(s->stream, sf.ev_in[ns - 1], 0));
-            x.prim(0, b[0], b[1] - b[0]);
-            if (ns > 1) x.prim(0, b[ns - 1], b[ns] - b[ns - 1]);
-        } else {
-            x.prim(rk, 0, nz);
+    int nd = 0;
+    for (const SlabOp &o : sf.plan->ops) {
+        const int n = o.b - o.a;
+        switch (o.kind) {
+        case SP_UPLOAD:
+            if (int rc = copy(sf.cs, o.a, o.b, true)) return rc;
+            MLAU_CUDA(cudaEventRecord(sf.ev_up[o.n], sf.cs));
+            break;
+        case SP_WAIT: MLAU_CUDA(cudaStreamWaitEvent(s->stream, sf.ev_up[o.n], 0)); break;
+        case SP_PRIM: x.prim(o.rk, o.a, n); break;
+        case SP_AUX: x.aux(o.a, n); break;
+        case SP_SWEEP_X: x.sweep(0, o.a, o.b); break;
+        case SP_SWEEP_Y: x.sweep(1, o.a, o.b); break;
+        case SP_SWEEP_Z: x.sweep(2, o.a, o.b); break;
+        case SP_EMF: x.emf(o.a, n); break;
+        case SP_UPDATE: x.update(o.rk, dt, o.a, n); break;
+        case SP_DOWNLOAD:
+            MLAU_CUDA(cudaEventRecord(sf.ev_dn[nd], s->stream));
+            MLAU_CUDA(cudaStreamWaitEvent(sf.cd, sf.ev_dn[nd], 0));
+            nd++;
+            if (int rc = copy(sf.cd, o.a, o.b, false)) return rc;
+            break;
+        case SP_STAGE:
+            x.prim(o.rk, 0, nz);
+            x.aux(0, nz);
+            x.sweeps();
+            x.emf(0, nz);
+            x.update(o.rk, dt, oz, Nz);
+            break;
+        default: set_error("split3d_step_host: bad plan op"); return MLAU_ERR_ARG;
         }
-        x.aux();
-        x.sweeps();
-        x.emf();
-        if (rk + 1 < s->nrk) {
-            x.update(rk, dt, oz, Nz);
-        } else {
-            for (int c = 0; c < ns; c++) {
-                const int k0 = std::max(b[c], oz), k1 = std::min(b[c + 1], nz - oz);
-                x.update(rk, dt, k0, k1 - k0);
-                MLAU_CUDA(cudaEventRecord(sf.ev_out[c], s->stream));
-                MLAU_CUDA(cudaStreamWaitEvent(sf.cs, sf.ev_out[c], 0));
-                if (int rc = copy(k0, k1, false)) return rc;
-            }
-            if (int rc = copy(0, oz, false)) return rc;
-            if (int rc = copy(nz - oz, nz, false)) return rc;
-        }
-        MLAU_CUDA(cudaGetLastError());
     }
+    MLAU_CUDA(cudaGetLastError());
+    MLAU_CUDA(cudaStreamSynchronize(sf.cd));
     MLAU_CUDA(cudaStreamSynchronize(sf.cs));
     return split3d_check(s);
 }

@@ -356,12 +356,15 @@ WALL_CASES = [((24, 18), KHI, "lhlld"), ((32, 24), XWALLS, "mlau"), ((20, 28), B
 
 
 def wall_cases(port, seed=76):
-    """States whose pressure stays positive over the tests' 20 steps with
-    these tables (checked with the oracle; the engine retires an instance
-    whose pressure goes non-positive, the single-instance step does not)."""
+    """Subsonic states for these tables: over the tests' 20 steps the local
+    Mach number stays below 0.65 and the pressure above 0.24 (checked with the
+    oracle).  Below Mach 1 the split engine reconstructs in its Alfven-wave
+    form, whose FP32 error the 1e-6 bound covers; transonic states switch to
+    the full 7-wave projection, held to 1e-5 (tests/test_gpu_split.py)."""
     out = []
     for k, (shape, tables, flux) in enumerate(WALL_CASES):
-        st, m = ics.turbulence_2d(n=shape[0], ny=shape[1], seed=seed + k, vrms=0.25)
+        st, m = ics.turbulence_2d(n=shape[0], ny=shape[1], seed=seed + k, vrms=0.2, beta=4.0,
+                                  kmax=4)
         port.setbc2d(st, *tables)
         out.append(dict(st=st, m=m, tables=tables, flux=flux))
     return out

@@ -98,26 +98,47 @@ def test_split_ghosts_are_periodic_images(prec):
         assert np.array_equal(np.pad(inner, 4, mode="wrap"), a), k
 
 
-@pytest.mark.parametrize("shape,prec", [((12, 16, 16), M.FP32_SPLIT), ((16, 16, 16), M.FP32_SPLIT),
-                                        ((24, 16, 40), M.FP32_SPLIT), ((32, 32, 32), M.FP32_SPLIT),
-                                        ((72, 24, 20), M.FP32_SPLIT), ((24, 16, 40), M.FP32_SPLIT_F64),
-                                        ((72, 24, 20), M.FP32_SPLIT_F64)])
-def test_split_dropin_driver(shape, prec):
-    """mhd_fd_ct_3d in FP32-split mode overlaps its host copies with the step
-    (z-slabs: 1, 2, 3, 4 and 8 of them here, ghost planes last); two calls in a
-    row equal two handle-API steps bit for bit."""
-    nzi, nyi, nxi = shape
-    st, m = ics.turbulence_3d(n=nxi, ny=nyi, nz=nzi, mach=1e-2, seed=4)
+def dropin_steps(st, m, prec, nrk, calls):
     nz, ny, nx = st["ro"].shape
-    ref = run(st, m, 2, 1e-3, prec)
-    M.set_scheme(3, 4, "mlau", 3)
+    M.set_scheme(3, 4, "mlau", nrk)
     M.set_precision(3, prec)
     try:
-        for _ in range(2):
+        for _ in range(calls):
             M.mhd_fd_ct_3d(*[st[k] for k in ("ro", "mx", "my", "mz", "en", "bx", "by", "bz")],
                            1e-3, m["dx"], m["dy"], m["dz"], nx, ny, nz, 4, 4, 4, m["gamma"])
     finally:
         M.set_precision(3, M.FP64)
+        M.set_scheme(3, 4, "mlau", 3)
         M.release_dropin()
+
+
+@pytest.mark.parametrize("shape,prec", [((12, 16, 16), M.FP32_SPLIT), ((16, 16, 16), M.FP32_SPLIT),
+                                        ((24, 16, 40), M.FP32_SPLIT), ((32, 32, 32), M.FP32_SPLIT),
+                                        ((72, 24, 20), M.FP32_SPLIT), ((136, 12, 16), M.FP32_SPLIT),
+                                        ((24, 16, 40), M.FP32_SPLIT_F64),
+                                        ((72, 24, 20), M.FP32_SPLIT_F64)])
+def test_split_dropin_driver(shape, prec):
+    """mhd_fd_ct_3d in FP32-split mode runs the step over z-plane ranges so
+    that its host copies overlap the first and last RK stages (1, 2, 4 and 8
+    slabs here; the plan is checked on the CPU by tests/test_slab_plan.py);
+    two calls in a row equal two handle-API steps bit for bit."""
+    nzi, nyi, nxi = shape
+    st, m = ics.turbulence_3d(n=nxi, ny=nyi, nz=nzi, mach=1e-2, seed=4)
+    ref = run(st, m, 2, 1e-3, prec)
+    dropin_steps(st, m, prec, 3, 2)
+    for k in ref:
+        assert np.array_equal(st[k], ref[k]), k
+
+
+@pytest.mark.parametrize("nrk", (1, 2))
+def test_split_dropin_driver_other_rk(nrk):
+    """The same with RK1 (uploads and downloads in one stage) and RK2."""
+    st, m = ics.turbulence_3d(n=20, ny=24, nz=72, mach=1e-2, seed=6)
+    with M.Sim(3, st["ro"].shape, dx=m["dx"], dy=m["dy"], dz=m["dz"], odr=4, flux="mlau",
+               nrk=nrk, precision=M.FP32_SPLIT) as s:
+        s.upload(st)
+        s.step(1e-3, 2)
+        ref = s.download()
+    dropin_steps(st, m, M.FP32_SPLIT, nrk, 2)
     for k in ref:
         assert np.array_equal(st[k], ref[k]), k
