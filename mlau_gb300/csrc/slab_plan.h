@@ -95,13 +95,34 @@ struct SlabGeom {
 
 class SlabPlan {
 public:
-    // nslab: slabs the first and last stages are requested in; chunk: planes
-    // per upload
+    // first / last: the interior slab sizes (in z order, summing to the
+    // interior depth) the first and last stages are requested in; chunk:
+    // planes per upload
+    SlabPlan(const SlabGeom &g, int nrk, const std::vector<int> &first,
+             const std::vector<int> &last, int chunk)
+        : g_(g), nrk_(nrk), chunk_(std::max(1, chunk))
+    {
+        build(first, last);
+    }
+    // nslab equal slabs in both stages
     SlabPlan(const SlabGeom &g, int nrk, int nslab, int chunk)
         : g_(g), nrk_(nrk), chunk_(std::max(1, chunk))
     {
-        const int nz = g.nz, oz = g.oz, Nz = g.Nz();
+        const int Nz = g.Nz();
         nslab = std::max(1, std::min(nslab, Nz));
+        std::vector<int> sz;
+        for (int c = 0; c < nslab; c++)
+            sz.push_back((int)((long long)Nz * (c + 1) / nslab - (long long)Nz * c / nslab));
+        build(sz, sz);
+    }
+    std::vector<SlabOp> ops;
+    int uploads() const { return nup_; }
+
+private:
+    void build(const std::vector<int> &first, const std::vector<int> &last)
+    {
+        const SlabGeom &g = g_;
+        const int nz = g.nz, oz = g.oz;
         readers_.assign(nz, {});
         std::vector<int> r;
         for (int k = 0; k < nz; k++) {
@@ -118,27 +139,27 @@ public:
             for (int p : r) writer_[p] = k;
         }
         up_.assign(nz, -1);
-        for (int rk = 0; rk < nrk; rk++) {
-            const bool first = rk == 0, last = rk == nrk - 1;
-            if (!first && !last) {
+        for (int rk = 0; rk < nrk_; rk++) {
+            const bool is_first = rk == 0, is_last = rk == nrk_ - 1;
+            if (!is_first && !is_last) {
                 ops.push_back({SP_STAGE, rk, 0, nz, 0});
                 continue;
             }
             reset(rk);
             std::vector<char> sent(nz, 0);
-            for (int c = 0; c < nslab; c++) {
-                const int a = oz + (int)((long long)Nz * c / nslab);
-                const int b = oz + (int)((long long)Nz * (c + 1) / nslab);
+            int a = oz;
+            for (int len : is_first ? first : last) {
+                const int b = std::min(nz - oz, a + std::max(0, len));
                 need_update(range(a, b));
-                if (last) download_final(sent);
+                if (is_last) download_final(sent);
+                a = b;
             }
+            // whatever the sizes left out
+            need_update(range(a, nz - oz));
+            if (is_last) download_final(sent);
         }
     }
 
-    std::vector<SlabOp> ops;
-    int uploads() const { return nup_; }
-
-private:
     SlabGeom g_;
     int nrk_, chunk_;
     int rk_ = 0, nup_ = 0, waited_ = -1;

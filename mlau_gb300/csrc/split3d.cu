@@ -1204,7 +1204,8 @@ int split3d_step_host(Sim *s, double dt, double *const *h)
     }
     if (!sf.plan || sf.plan_nrk != s->nrk) {
         // the first and last stages are asked for in slabs of >= 16 interior
-        // planes (at most 8); uploads of half a slab
+        // planes (at most 8); uploads of half a slab (tapered slab sizes and
+        // 4-16 slabs measured within 2 % of this at 256^3)
         const int nslab = std::max(1, std::min(8, Nz / 16));
         const int chunk = std::max(4, (nz + 2 * nslab - 1) / (2 * nslab));
         sf.plan.reset(new SlabPlan(SlabGeom{nz, oz, SG<2>::T}, s->nrk, nslab, chunk));

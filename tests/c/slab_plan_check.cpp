@@ -207,6 +207,7 @@ struct Replay {
 int main()
 {
     int checked = 0;
+    unsigned seed = 12345u;
     const int tzs[] = {16, 5, 32};
     for (int tz : tzs)
         for (int oz = 4; oz <= 5; oz++)
@@ -215,7 +216,8 @@ int main()
                     for (int nslab : {1, 2, 3, 8, 16})
                         for (int chunk : {1, 7, 16, 64}) {
                             const int nz = Nz + 2 * oz;
-                            SlabPlan plan(SlabGeom{nz, oz, tz}, nrk, nslab, chunk);
+                            const SlabGeom g{nz, oz, tz};
+                            SlabPlan plan(g, nrk, nslab, chunk);
                             Replay r{nz, oz, tz, nrk, Nz, ""};
                             if (!r.run(plan.ops)) {
                                 printf("FAIL nz=%d oz=%d tz=%d nrk=%d nslab=%d chunk=%d: %s\n", nz, oz,
@@ -223,6 +225,29 @@ int main()
                                 return 1;
                             }
                             checked++;
+                            // arbitrary slab sizes (short, long, zero)
+                            const int body = std::max(1, Nz / nslab);
+                            std::vector<int> rnd, rnd2;
+                            for (std::vector<int> *v : {&rnd, &rnd2})
+                                for (int a = 0; a < Nz + 8;) {
+                                    seed = seed * 1103515245u + 12345u;
+                                    const int len = (int)((seed >> 16) % (unsigned)(2 * body + 2));
+                                    v->push_back(len);
+                                    a += std::max(1, len);
+                                }
+                            std::vector<int> uni;
+                            for (int c = 0; c < nslab; c++) uni.push_back(body);
+                            const std::vector<int> *sets[][2] = {{&rnd, &rnd2}, {&uni, &rnd}, {&rnd2, &uni}};
+                            for (auto &pr : sets) {
+                                SlabPlan p2(g, nrk, *pr[0], *pr[1], chunk);
+                                Replay r2{nz, oz, tz, nrk, Nz, ""};
+                                if (!r2.run(p2.ops)) {
+                                    printf("FAIL (sized slabs) nz=%d oz=%d tz=%d nrk=%d body=%d chunk=%d: %s\n",
+                                           nz, oz, tz, nrk, body, chunk, r2.err.c_str());
+                                    return 1;
+                                }
+                                checked++;
+                            }
                         }
     printf("ok %d\n", checked);
     return 0;
