@@ -407,12 +407,12 @@ __device__ __forceinline__ void issue_tile(const SweepMaps &M, unsigned char *st
 }
 
 // Per-cell results of a sweep tile in shared memory: sl / sr - the face
-// perturbations at the cell's right / left face plus the two central CT parts;
-// sb - the cell-centre state as (hi, lo).
+// perturbations at the cell's right / left face plus the two central CT parts.
+// (The cell-centre states the Riemann step needs are read from the staged
+// tile itself: a face's two cells are its thread's stencil points 1 and 2.)
 template <int D> struct CellSmem {
     float (&sl)[9][SG<D>::TB][SG<D>::TA];
     float (&sr)[9][SG<D>::TB][SG<D>::TA];
-    float2 (&sb)[7][SG<D>::TB][SG<D>::TA];
 };
 
 // Reconstruction of one cell, any scheme: characteristic projection of the
@@ -441,7 +441,6 @@ __device__ __forceinline__ void rec_cell(const float2 *Q, const float *Fs, const
             z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
         }
         if (z) zero |= 1u << n;
-        c.sb[n][tb][ta] = h[2];
     }
     float ul[7], ur[7];
     const float2 bn2 = QI(SQ_BN, 2);
@@ -506,7 +505,6 @@ __device__ __forceinline__ void rec_cell_wcns4(const float2 *Q, const float *Fs,
 #pragma unroll
         for (int m = 0; m < 5; m++) z = z && (h[m].x == 0.f) && (h[m].y == 0.f);
         if (z) zero |= 1u << n;
-        c.sb[n][tb][ta] = h[2];
     }
     const float2 bn2 = QI(SQ_BN, 2);
     const float bnc = bn2.x + bn2.y;
@@ -559,9 +557,8 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
     unsigned char *stages =
         (unsigned char *)(((uintptr_t)dyn_smem + 127) & ~(uintptr_t)127);
     // per-cell results: sl/sr - perturbation at the cell's right / left face
-    // + 2 central parts; sb - the cell-centre state as (hi, lo)
+    // + 2 central parts
     __shared__ float sl[9][TB][TA], sr[9][TB][TA];
-    __shared__ float2 sb[7][TB][TA];
     __shared__ uint64_t bar[2];
     const int ta = threadIdx.x, tb = threadIdx.y, tid = tb * TA + ta;
     const int p = (D == 0) ? ta : tb;  // position along the sweep inside the tile
@@ -605,7 +602,7 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
         auto FI = [&](int n, int m) { return Fs[n * NB + bidx<D>(a, ta, tb, m)]; };
 
         if (do_rec) {
-            const CellSmem<D> cs{sl, sr, sb};
+            const CellSmem<D> cs{sl, sr};
             if constexpr (ODR == 4) rec_cell_wcns4<D>(Q, Fs, a, ta, tb, odr, gamma, cs);
             else rec_cell<D>(Q, Fs, a, ta, tb, odr, gamma, cs);
         }
@@ -613,22 +610,25 @@ ks_sweep(const __grid_constant__ SweepMaps M, SplitPtrs g, Dims d, int odr_rt, i
 
         if (in_box && p >= 1 && ac >= 3 && ac < len - 2) {
             const int tbl = (D == 0) ? tb : tb - 1, tal = (D == 0) ? ta - 1 : ta;
+            // the two cells' centre states: stencil points 1 (left) and 2 (right)
+            float2 cl[7], cr[7];
             float L[7], Rr[7];
 #pragma unroll
             for (int n = 0; n < 7; n++) {
-                L[n] = (sb[n][tbl][tal].x + sb[n][tbl][tal].y) + sl[n][tbl][tal];
-                Rr[n] = (sb[n][tb][ta].x + sb[n][tb][ta].y) + sr[n][tb][ta];
+                cl[n] = QI(n, 1);
+                cr[n] = QI(n, 2);
+                L[n] = (cl[n].x + cl[n].y) + sl[n][tbl][tal];
+                Rr[n] = (cr[n].x + cr[n].y) + sr[n][tb][ta];
             }
             // jumps from split parts: centre difference from the pairs, plus
             // the difference of the FP32 perturbations
             auto jump = [&](int n) {
-                return ((sb[n][tb][ta].x - sb[n][tbl][tal].x) + (sb[n][tb][ta].y - sb[n][tbl][tal].y))
-                       + (sr[n][tb][ta] - sl[n][tbl][tal]);
+                return ((cr[n].x - cl[n].x) + (cr[n].y - cl[n].y)) + (sr[n][tb][ta] - sl[n][tbl][tal]);
             };
             const float jv = jump(1);
             const float jp = jump(6) + 0.5f * (jump(4) * (Rr[4] + L[4]) + jump(5) * (Rr[5] + L[5]));
             const float bn = FI(SF_BF, 2);
-            const float dv0 = (sb[1][tb][ta].x - sb[1][tbl][tal].x) + (sb[1][tb][ta].y - sb[1][tbl][tal].y);
+            const float dv0 = (cr[1].x - cl[1].x) + (cr[1].y - cl[1].y);
             const float dvtm = fminf(fminf(FI(SF_DVT, 1), FI(SF_DVT, 2)),
                                      fminf(FI(SF_DVU, 1), FI(SF_DVU, 2)));
             float F[7];
