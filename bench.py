@@ -544,7 +544,7 @@ def run_step1d(args):
     """Config C0: 1D Riemann problem, 2048 cells, MLAU + MUSCL (minmod) + RK3,
     gamma=2, CFL 0.4, open boundaries, dt fixed from the initial state, run to
     t_end=0.1 as the 1D driver does; the whole run is timed (one problem is
-    launch-latency bound: 13 launches per step)."""
+    latency bound: 11 launches per step, the open boundary beside the first stage)."""
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     import mlau_gb300 as M
     from mlau_gb300 import ics
@@ -579,7 +579,7 @@ def run_step1d(args):
                        "time_to_solution_ms": ms, "l2": "fits in L2 (one resident problem)"},
             "roofline": None,
             "roofline_note": "latency bound: each warp's FP64 chain (a warp FP64 instruction holds "
-                             "its sub-partition's pipe 64 cycles) and 13 launches per step",
+                             "its sub-partition's pipe 64 cycles) and 11 launches per step",
             "gpu_launches": launches, "clocks": clk.summary(),
             "cpu_baseline": {"value": cv, "unit": UNIT,
                              "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",

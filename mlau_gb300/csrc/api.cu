@@ -113,7 +113,9 @@ int launches_per_step(const Sim *s)
     if (s->sp) return s->nrk * (s->walls3d ? 9 : 7);
     if (s->g.dim == 3) return s->nrk * (s->walls3d ? 12 : 10);
     if (s->g.dim == 2) return s->nrk * (s->walls2d ? 10 : 8);
-    return s->nrk * 4 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
+    // 1D: primitives once per step (the later stages' come from the update),
+    // reconstruction, flux and update per stage, the open boundary once
+    return 1 + s->nrk * 3 + (s->bc1d == MLAU_BC1D_OPEN ? 1 : 0);
 }
 
 }  // namespace mlau
@@ -186,6 +188,12 @@ int mlau_sim_destroy(mlau_sim *s)
     diff2d_free(s);
     if (s->sp) split3d_free(s);
     for (void *p : s->allocs) cudaFree(p);
+    if (s->stream2) {
+        cudaStreamSynchronize(s->stream2);
+        cudaStreamDestroy(s->stream2);
+        cudaEventDestroy(s->ev_fork);
+        cudaEventDestroy(s->ev_join);
+    }
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return MLAU_OK;

@@ -21,8 +21,10 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
 namespace {
 
 constexpr int kMaxNx = MLAU_NOALLOC_1D_MAX_NX;
-// u0 (7 x nx) + vx, vy, vz, pr (4 x nx) + face states (14 x (nx+1)) + fluxes (7 x nx)
+// u0 (7 x nx) + vx, vy, vz, pr (4 x nx) + face states (14 x (nx+1)) + fluxes
+// (7 x nx) + the open boundary's two ghost states (14): 32 nx + 28 doubles
 constexpr long long kScratch = 32LL * (kMaxNx + 1);
+static_assert(32LL * kMaxNx + 28 <= kScratch, "noalloc scratch too small");
 
 // One array per process and device; it lives until the process exits.
 static __device__ __align__(256) double g_noalloc_scratch[kScratch];
@@ -98,6 +100,7 @@ extern "C" int mlau_fd4c_1d_noalloc(double *ro, double *mx, double *my, double *
     for (int v = 0; v < 7; v++) { f.ul[v] = p; p += nx + 1; }
     for (int v = 0; v < 7; v++) { f.ur[v] = p; p += nx + 1; }
     for (int v = 0; v < 7; v++) { f.F[0][v] = p; p += nx; }
+    f.obc = p;
     return plain1d_enqueue(f, nx, xoff, odr, flux, nrk, bc, bx, dt, dx, gamma,
                            (cudaStream_t)stream);
 }

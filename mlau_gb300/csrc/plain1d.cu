@@ -11,8 +11,23 @@
 namespace mlau {
 namespace {
 
-// Primitives; at the first stage also the copy of the state U^n (seven small
-// copies would cost more than the kernel).
+// Primitives of cell i from its conserved state (ro, mx, my, mz, by, bz, en).
+__device__ __forceinline__ void put_prim1(const PlainFields &f, int i, double ro, double mx,
+                                          double my, double mz, double by, double bz, double en,
+                                          double bx, double gamma)
+{
+    const double iro = 1.0 / ro;
+    const double vx = mx * iro, vy = my * iro, vz = mz * iro;
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    const double b2 = bx * bx + by * by + bz * bz;
+    f.vx[i] = vx;
+    f.vy[i] = vy;
+    f.vz[i] = vz;
+    f.pr[i] = (gamma - 1) * (en - 0.5 * (ro * v2 + b2));
+}
+
+// Primitives and the copy of the state U^n, at the first stage of a step (the
+// later stages take their primitives from the update before them).
 __global__ void k_prim1(PlainFields f, int nx, double bx, double gamma, int save_u0)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -20,15 +35,8 @@ __global__ void k_prim1(PlainFields f, int nx, double bx, double gamma, int save
     if (save_u0)
         for (int v = 0; v < 8; v++)
             if (v != 5) f.u0[v][i] = f.s[v][i];
-    const double ro = f.s[0][i], iro = 1.0 / ro;
-    const double vx = f.s[1][i] * iro, vy = f.s[2][i] * iro, vz = f.s[3][i] * iro;
-    const double by = f.s[6][i], bz = f.s[7][i];
-    const double v2 = vx * vx + vy * vy + vz * vz;
-    const double b2 = bx * bx + by * by + bz * bz;
-    f.vx[i] = vx;
-    f.vy[i] = vy;
-    f.vz[i] = vz;
-    f.pr[i] = (gamma - 1) * (f.s[4][i] - 0.5 * (ro * v2 + b2));
+    put_prim1(f, i, f.s[0][i], f.s[1][i], f.s[2][i], f.s[3][i], f.s[6][i], f.s[7][i], f.s[4][i],
+              bx, gamma);
 }
 
 // Face states (:133-186): full characteristic system where any of the three
@@ -368,8 +376,8 @@ __global__ void k_openbc1(PlainFields f, int nx, int xoff, double bx, double dtd
     const int r = threadIdx.x;
     if (blockIdx.x > 1 || r >= 8) return;  // launched with 8 threads per block
     const int n = r < 7 ? r : 6;
-    double *ro = f.s[0], *mx = f.s[1], *my = f.s[2], *mz = f.s[3], *en = f.s[4], *by = f.s[6],
-           *bz = f.s[7];
+    const double *ro = f.s[0], *mx = f.s[1], *my = f.s[2], *mz = f.s[3], *en = f.s[4],
+                 *by = f.s[6], *bz = f.s[7];
     const double bx2 = bx * bx;
     const int side = blockIdx.x;
     const int sgn = side ? -1 : 1;
@@ -408,39 +416,43 @@ __global__ void k_openbc1(PlainFields f, int nx, int xoff, double bx, double dtd
     double p[7];
     for (int k = 0; k < 7; k++) p[k] = __shfl_sync(0xffu, pn, k, 8);
     if (r != 0) return;
-    ro[so] = p[0];
-    mx[so] = p[1];
-    my[so] = p[2];
-    mz[so] = p[3];
-    by[so] = p[4];
-    bz[so] = p[5];
-    en[so] = p[6];
-    const double v2 = mx[so] * mx[so] + my[so] * my[so] + mz[so] * mz[so];
-    const double b2 = bx2 + by[so] * by[so] + bz[so] * bz[so];
-    en[so] = en[so] / (gamma - 1.0) + 0.5 * (ro[so] * v2 + b2);
-    mx[so] *= ro[so];
-    my[so] *= ro[so];
-    mz[so] *= ro[so];
-    for (int j = 0; j < xoff - 1; j++) {
-        const int s = side * (nx - 1) + sgn * j;
-        ro[s] = ro[so];
-        mx[s] = mx[so];
-        my[s] = my[so];
-        mz[s] = mz[so];
-        by[s] = by[so];
-        bz[s] = bz[so];
-        en[s] = en[so];
-    }
+    // conserved ghost state, in the reference's order of operations
+    const double v2 = p[1] * p[1] + p[2] * p[2] + p[3] * p[3];
+    const double b2 = bx2 + p[4] * p[4] + p[5] * p[5];
+    double *o = f.obc + 7 * side;
+    o[0] = p[0];
+    o[1] = p[1] * p[0];
+    o[2] = p[2] * p[0];
+    o[3] = p[3] * p[0];
+    o[4] = p[4];
+    o[5] = p[5];
+    o[6] = p[6] / (gamma - 1.0) + 0.5 * (p[0] * v2 + b2);
 }
 
 // Update (:220-255); with periodic boundaries each cell also writes its ghost
-// images (prdc_1d, 1D/SERIAL/wave/prdc_1d.c).
+// images (prdc_1d, 1D/SERIAL/wave/prdc_1d.c).  openbc: the first stage of an
+// open-boundary step, whose ghost cells take the states k_openbc1 left in
+// f.obc (every ghost cell of a side the same, openbc1d_mhd.c:160-175); the
+// first and last interior threads write them.  Every cell written also gets
+// its primitives (k_prim1's arithmetic), which the next stage reads; ghost
+// cells an open boundary leaves alone keep those of the first stage.
 __global__ void k_update1(PlainFields f, int nx, int xoff, int odr, double ra, double rb,
-                          double dtdx, int periodic)
+                          double dtdx, int periodic, int openbc, double bx, double gamma)
 {
     const int i = xoff + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx - xoff) return;
     const int sv[7] = {0, 1, 2, 3, 6, 7, 4};  // flux order (ro, mx, my, mz, by, bz, en)
+    if (openbc && (i == xoff || i == nx - xoff - 1)) {
+        const int side = i == xoff ? 0 : 1;
+        const int g0 = side ? nx - xoff : 0;
+        double g[7];
+        for (int v = 0; v < 7; v++) {
+            g[v] = f.obc[7 * side + v];
+            for (int j = 0; j < xoff; j++) f.s[sv[v]][g0 + j] = g[v];
+        }
+        for (int j = 0; j < xoff; j++)
+            put_prim1(f, g0 + j, g[0], g[1], g[2], g[3], g[4], g[5], g[6], bx, gamma);
+    }
     double out[7];
 #pragma unroll
     for (int v = 0; v < 7; v++) {
@@ -454,6 +466,7 @@ __global__ void k_update1(PlainFields f, int nx, int xoff, int odr, double ra, d
         if (im[a] < 0) continue;
 #pragma unroll
         for (int v = 0; v < 7; v++) f.s[sv[v]][im[a]] = out[v];
+        put_prim1(f, im[a], out[0], out[1], out[2], out[3], out[4], out[5], out[6], bx, gamma);
     }
 }
 
@@ -469,7 +482,13 @@ int plain1d_alloc(Sim *s)
     for (auto p : singles) rc |= dalloc(s, p, n);
     for (int v = 0; v < 7; v++)
         rc |= dalloc(s, &f.ul[v], n + 1) | dalloc(s, &f.ur[v], n + 1) | dalloc(s, &f.F[0][v], n);
-    return rc ? MLAU_ERR_NOMEM : MLAU_OK;
+    rc |= dalloc(s, &f.obc, 14);
+    if (rc) return MLAU_ERR_NOMEM;
+    // created here, not at the first step, which may be inside a graph capture
+    MLAU_CUDA(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
+    MLAU_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    MLAU_CUDA(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    return MLAU_OK;
 }
 
 // 1D grids hold a few thousand cells, each cell a long chain of FP64
@@ -487,12 +506,24 @@ int plain1d_step(Sim *s, double dt)
     const int nx = g.nx, off = g.ox;
     const double dtdx = dt / g.dx;
     const int T = T1D;
+    const bool open = s->bc1d == MLAU_BC1D_OPEN;
+    // The open boundary reads only the state of its two end cells, which no
+    // kernel of the first stage writes before the update: it runs on a second
+    // stream beside the stage (forked here, joined before the update; one
+    // stream when the kernels are timed one by one).
+    const bool fork = open && !s->timer.on && s->stream2;
     for (int rk = 0; rk < s->nrk; rk++) {
         double ra, rb;
         rk_coef(s->nrk, rk, ra, rb);
-        {
+        if (fork && rk == 0) {
+            MLAU_CUDA(cudaEventRecord(s->ev_fork, st));
+            MLAU_CUDA(cudaStreamWaitEvent(s->stream2, s->ev_fork, 0));
+            k_openbc1<<<2, 8, 0, s->stream2>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
+            MLAU_CUDA(cudaEventRecord(s->ev_join, s->stream2));
+        }
+        if (rk == 0) {
             TimedLaunch tl(&s->timer, KK_PRIM);
-            k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, s->bx1d, s->gamma, rk == 0);
+            k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, s->bx1d, s->gamma, 1);
         }
         {
             TimedLaunch tl(&s->timer, KK_REC);
@@ -507,14 +538,19 @@ int plain1d_step(Sim *s, double dt)
             else
                 k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, s->flux, s->bx1d, s->gamma);
         }
-        if (s->bc1d == MLAU_BC1D_OPEN && rk == 0) {
-            TimedLaunch tl(&s->timer, KK_AUX);
-            k_openbc1<<<2, 8, 0, st>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
+        if (open && rk == 0) {
+            if (fork) {
+                MLAU_CUDA(cudaStreamWaitEvent(st, s->ev_join, 0));
+            } else {
+                TimedLaunch tl(&s->timer, KK_AUX);
+                k_openbc1<<<2, 8, 0, st>>>(f, nx, off, s->bx1d, dtdx, s->gamma);
+            }
         }
         {
             TimedLaunch tl(&s->timer, KK_UPDATE);
             k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(
-                f, nx, off, s->odr, ra, rb, dtdx, s->bc1d == MLAU_BC1D_PERIODIC);
+                f, nx, off, s->odr, ra, rb, dtdx, s->bc1d == MLAU_BC1D_PERIODIC, open && rk == 0,
+                s->bx1d, s->gamma);
         }
         MLAU_CUDA(cudaGetLastError());
     }
@@ -536,7 +572,7 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
     for (int rk = 0; rk < nrk; rk++) {
         double ra, rb;
         rk_coef(nrk, rk, ra, rb);
-        k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma, rk == 0);
+        if (rk == 0) k_prim1<<<blocks_for(nx, T), T, 0, st>>>(f, nx, bx, gamma, 1);
         k_rec1<<<blocks_for((long long)(nx - 4) * RLANES, T), T, 0, st>>>(f, nx, odr, EIG_FULL,
                                                                         bx, gamma);
         if (flux == FLUX_MLAU)
@@ -545,7 +581,9 @@ int plain1d_enqueue(const PlainFields &f, int nx, int off, int odr, int flux, in
             k_flux1<<<blocks_for(nx - 5, T), T, 0, st>>>(f, nx, flux, bx, gamma);
         if (bc == MLAU_BC1D_OPEN && rk == 0) k_openbc1<<<2, 8, 0, st>>>(f, nx, off, bx, dtdx, gamma);
         k_update1<<<blocks_for(nx - 2 * off, T), T, 0, st>>>(f, nx, off, odr, ra, rb, dtdx,
-                                                            bc == MLAU_BC1D_PERIODIC);
+                                                            bc == MLAU_BC1D_PERIODIC,
+                                                            bc == MLAU_BC1D_OPEN && rk == 0, bx,
+                                                            gamma);
         MLAU_CUDA(cudaGetLastError());
     }
     return MLAU_OK;

@@ -17,6 +17,7 @@ struct PlainFields {
     double *F[3][7];     // face fluxes per direction: (ro, mn, mt, mu, bt, bu, en)
     double *FC[3][2];    // central parts of the bt and bu fluxes
     double *e[3];        // edge EMFs ex, ey, ez
+    double *obc;         // 1D open boundary: each side's ghost state (ro, mx, my, mz, by, bz, en)
 };
 
 struct Geometry {
@@ -46,6 +47,10 @@ struct Sim {
     Bc3 bc3{};           // 3D boundary tables (all zero: periodic)
     bool walls3d = false;  // some 3D table entry is not periodic
     cudaStream_t stream = nullptr;
+    // 1D open boundary: a second stream and fork / join events, so that the
+    // boundary's serial chain runs beside the first stage's kernels
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     PlainFields f{};
     SplitFields *sp = nullptr;
     std::vector<void *> allocs;
