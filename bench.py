@@ -826,6 +826,18 @@ def main():
                 samples[name] = {k: r2.get(k) for k in ("metric", "value", "unit", "ms_per_step",
                                                         "steps", "config", "cpu_baseline",
                                                         "roofline")}
+            # and the serving loop on a bounded request stream (12 requests at
+            # 50 req/s, reduced sizes), against one-at-a-time FP64
+            a3 = argparse.Namespace(**vars(args))
+            a3.serve_n, a3.rates = 12, "50"
+            a3.serve_n1d_max, a3.serve_n2d_max, a3.serve_n3d_max = 4096, 256, 64
+            a3.serve_t_end_max = 0.2
+            try:
+                sv = run_serve(a3)
+                samples["serve"] = {k: sv.get(k) for k in ("metric", "unit", "p50_s", "p99_s",
+                                                           "config", "rates")}
+            except Exception as e:  # the headline line must not depend on the sample
+                samples["serve"] = {"error": f"{type(e).__name__}: {e}"}
             line["config_samples"] = samples
         if args.accuracy_steps > 0 and R.world == 1 and args.precision == "both":
             # the configuration's 200-step accuracy record at both Mach numbers
