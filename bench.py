@@ -654,10 +654,11 @@ def run_serve(args):
     out = {"metric": "serving time-to-solution p50/p99 and zone-updates/s",
            "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "f64 | f32+f64",
            "data": "synthetic seeded Poisson request stream",
-           "config": {"workload": f"{args.serve_n} requests: 50% 1D Riemann N logU[256,16384], "
-                                  f"40% 2D periodic (sizes logU 64..1024, t_end U[0.05,0.5]), "
-                                  f"10% 3D periodic 64^3..128^3 x 200 steps; FP64 or FP32-split "
-                                  f"per request (1D in FP64)",
+           "config": {"workload": f"{args.serve_n} requests: 50% 1D Riemann N "
+                                  f"logU[256,{args.serve_n1d_max}], 40% 2D periodic (sizes logU "
+                                  f"64..{args.serve_n2d_max}, t_end U[0.05,{args.serve_t_end_max:g}]), "
+                                  f"10% 3D periodic 64^3..{args.serve_n3d_max}^3 x 200 steps; FP64 "
+                                  f"or FP32-split per request (1D in FP64)",
                       "budget_gb": args.budget_gb,
                       "ranges": {k: list(v) for k, v in kw.items() if k != "seed"}},
            "rates": {}}

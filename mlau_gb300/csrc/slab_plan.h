@@ -97,15 +97,18 @@ class SlabPlan {
 public:
     // first / last: the interior slab sizes (in z order, summing to the
     // interior depth) the first and last stages are requested in; chunk:
-    // planes per upload
+    // planes per upload; first_start: the slab the first stage asks for
+    // first, the others following cyclically (a slab away from the ends
+    // needs no periodic source at the far end, so fewer uploads before its
+    // update can run)
     SlabPlan(const SlabGeom &g, int nrk, const std::vector<int> &first,
-             const std::vector<int> &last, int chunk)
+             const std::vector<int> &last, int chunk, int first_start = 0)
         : g_(g), nrk_(nrk), chunk_(std::max(1, chunk))
     {
-        build(first, last);
+        build(first, last, first_start);
     }
     // nslab equal slabs in both stages
-    SlabPlan(const SlabGeom &g, int nrk, int nslab, int chunk)
+    SlabPlan(const SlabGeom &g, int nrk, int nslab, int chunk, int first_start = 0)
         : g_(g), nrk_(nrk), chunk_(std::max(1, chunk))
     {
         const int Nz = g.Nz();
@@ -113,13 +116,13 @@ public:
         std::vector<int> sz;
         for (int c = 0; c < nslab; c++)
             sz.push_back((int)((long long)Nz * (c + 1) / nslab - (long long)Nz * c / nslab));
-        build(sz, sz);
+        build(sz, sz, first_start);
     }
     std::vector<SlabOp> ops;
     int uploads() const { return nup_; }
 
 private:
-    void build(const std::vector<int> &first, const std::vector<int> &last)
+    void build(const std::vector<int> &first, const std::vector<int> &last, int first_start)
     {
         const SlabGeom &g = g_;
         const int nz = g.nz, oz = g.oz;
@@ -147,16 +150,23 @@ private:
             }
             reset(rk);
             std::vector<char> sent(nz, 0);
+            // slab boundaries in z order; whatever the sizes leave out is a
+            // last slab of its own
+            std::vector<std::pair<int, int>> slabs;
             int a = oz;
             for (int len : is_first ? first : last) {
                 const int b = std::min(nz - oz, a + std::max(0, len));
-                need_update(range(a, b));
-                if (is_last) download_final(sent);
+                slabs.push_back({a, b});
                 a = b;
             }
-            // whatever the sizes left out
-            need_update(range(a, nz - oz));
-            if (is_last) download_final(sent);
+            slabs.push_back({a, nz - oz});
+            const int n = (int)slabs.size();
+            const int c0 = is_first ? ((first_start % n) + n) % n : 0;
+            for (int c = 0; c < n; c++) {
+                const std::pair<int, int> &sl = slabs[(c0 + c) % n];
+                need_update(range(sl.first, sl.second));
+                if (is_last) download_final(sent);
+            }
         }
     }
 

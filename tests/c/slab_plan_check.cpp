@@ -217,7 +217,7 @@ int main()
                         for (int chunk : {1, 7, 16, 64}) {
                             const int nz = Nz + 2 * oz;
                             const SlabGeom g{nz, oz, tz};
-                            SlabPlan plan(g, nrk, nslab, chunk);
+                            SlabPlan plan(g, nrk, nslab, chunk, (Nz + nslab + chunk) % (nslab + 1));
                             Replay r{nz, oz, tz, nrk, Nz, ""};
                             if (!r.run(plan.ops)) {
                                 printf("FAIL nz=%d oz=%d tz=%d nrk=%d nslab=%d chunk=%d: %s\n", nz, oz,
@@ -239,7 +239,7 @@ int main()
                             for (int c = 0; c < nslab; c++) uni.push_back(body);
                             const std::vector<int> *sets[][2] = {{&rnd, &rnd2}, {&uni, &rnd}, {&rnd2, &uni}};
                             for (auto &pr : sets) {
-                                SlabPlan p2(g, nrk, *pr[0], *pr[1], chunk);
+                                SlabPlan p2(g, nrk, *pr[0], *pr[1], chunk, (int)(seed >> 20) % 7);
                                 Replay r2{nz, oz, tz, nrk, Nz, ""};
                                 if (!r2.run(p2.ops)) {
                                     printf("FAIL (sized slabs) nz=%d oz=%d tz=%d nrk=%d body=%d chunk=%d: %s\n",
