@@ -103,6 +103,30 @@ def test_1d_vs_oracle(port, odr, flux, bc):
     assert equal_values(got, ref, keys=ref.keys())
 
 
+@pytest.mark.parametrize("bc", ("open", "periodic"))
+@pytest.mark.parametrize("nrk", (1, 2, 3))
+def test_1d_rk_orders_graphs_and_timing(port, nrk, bc):
+    """1D with RK1-3: 20 steps (16 of them from a captured step graph, in
+    which the open boundary runs on a forked stream) and the same 20 steps
+    with per-kernel timing on (the open boundary in line) equal the oracle."""
+    st, m = ics.riemann_1d(n=80, seed=40 + nrk)
+    dt = port.dt1d(st, m["bx"], m["gamma"], 0.4, m["dx"])
+    ref = ics.copy_state(st)
+    for _ in range(20):
+        port.step1d(ref, m["bx"], dt, m["dx"], gamma=m["gamma"], odr=2, flux="mlau", nrk=nrk,
+                    bc=bc)
+    for timing in (False, True):
+        with M.Sim(1, st["ro"].shape, dx=m["dx"], gamma=m["gamma"], odr=2, flux="mlau",
+                   nrk=nrk) as s:
+            s.set_bx(m["bx"])
+            s.set_bc(bc)
+            s.upload(st)
+            s.set_timing(timing)
+            s.step(dt, 20)
+            got = s.download()
+        assert equal_values(got, ref, keys=ref.keys()), (timing, max_rel_diff(got, ref))
+
+
 @pytest.mark.parametrize("nrk", (1, 2, 3))
 def test_3d_rk_orders(port, nrk):
     st, m = ics.turbulence_3d(n=8, mach=0.4, seed=21)
