@@ -6,7 +6,8 @@
 // same bits).
 //
 // The plan is demand-driven.  The first stage asks for the update of one
-// z-slab after another; each request first asks for what the update reads
+// z-slab after another (from a chosen slab on, cyclically; the bottom slab
+// first at the last stage); each request first asks for what the update reads
 // (z fluxes and edge EMFs of the neighbouring planes, x / y fluxes of its
 // planes), each of those for its own inputs, down to the primitive recovery,
 // which asks for the copies of the state planes it reads.  Whatever is not
