@@ -1052,14 +1052,14 @@ int split3d_alloc(Sim *s)
 void split3d_free(Sim *s)
 {
     SplitFields *sf = s->sp;
-    if (sf && sf->cs) {
-        cudaStreamSynchronize(sf->cs);
-        cudaStreamSynchronize(sf->cd);
+    if (sf) {
+        if (sf->cs) cudaStreamSynchronize(sf->cs);
+        if (sf->cd) cudaStreamSynchronize(sf->cd);
         for (cudaEvent_t e : sf->ev_up) cudaEventDestroy(e);
         for (cudaEvent_t e : sf->ev_dn) cudaEventDestroy(e);
-        cudaEventDestroy(sf->ev_start);
-        cudaStreamDestroy(sf->cs);
-        cudaStreamDestroy(sf->cd);
+        if (sf->ev_start) cudaEventDestroy(sf->ev_start);
+        if (sf->cs) cudaStreamDestroy(sf->cs);
+        if (sf->cd) cudaStreamDestroy(sf->cd);
     }
     delete sf;
     s->sp = nullptr;
@@ -1197,11 +1197,9 @@ int split3d_step_host(Sim *s, double dt, double *const *h)
     const Geometry &G = s->g;
     SplitFields &sf = *s->sp;
     const int nz = G.nz, oz = G.oz, Nz = nz - 2 * oz;
-    if (!sf.cs) {
-        MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cs, cudaStreamNonBlocking));
-        MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cd, cudaStreamNonBlocking));
-        MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_start, cudaEventDisableTiming));
-    }
+    if (!sf.cs) MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cs, cudaStreamNonBlocking));
+    if (!sf.cd) MLAU_CUDA(cudaStreamCreateWithFlags(&sf.cd, cudaStreamNonBlocking));
+    if (!sf.ev_start) MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_start, cudaEventDisableTiming));
     if (!sf.plan || sf.plan_nrk != s->nrk) {
         // the first and last stages are asked for in slabs of >= 16 interior
         // planes (at most 8); uploads of half a slab (tapered slab sizes and
@@ -1215,14 +1213,21 @@ int split3d_step_host(Sim *s, double dt, double *const *h)
         sf.plan_nrk = s->nrk;
         int ndn = 0;
         for (const SlabOp &o : sf.plan->ops) ndn += o.kind == SP_DOWNLOAD;
-        for (size_t e = sf.ev_up.size(); e < (size_t)sf.plan->uploads(); e++) {
-            sf.ev_up.push_back(nullptr);
-            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_up.back(), cudaEventDisableTiming));
-        }
-        for (size_t e = sf.ev_dn.size(); e < (size_t)ndn; e++) {
-            sf.ev_dn.push_back(nullptr);
-            MLAU_CUDA(cudaEventCreateWithFlags(&sf.ev_dn.back(), cudaEventDisableTiming));
-        }
+        auto grow = [&](std::vector<cudaEvent_t> &v, size_t n) -> int {
+            while (v.size() < n) {
+                cudaEvent_t e = nullptr;
+                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                    sf.plan.reset();  // the next call builds the plan and its events again
+                    set_error("split3d_step_host: cudaEventCreate: %s",
+                              cudaGetErrorString(cudaGetLastError()));
+                    return MLAU_ERR_CUDA;
+                }
+                v.push_back(e);
+            }
+            return MLAU_OK;
+        };
+        if (int rc = grow(sf.ev_up, (size_t)sf.plan->uploads())) return rc;
+        if (int rc = grow(sf.ev_dn, (size_t)ndn)) return rc;
     }
     const long long plane = (long long)G.nx * G.ny;
     auto copy = [&](cudaStream_t st, int k0, int k1, bool in) -> int {
